@@ -1,0 +1,150 @@
+/*
+ * lbm_gb300.h -- C ABI of the GB300 (sm_103a) D2Q9 BGK lattice Boltzmann hot path.
+ *
+ * Every entry point is `extern "C"`, takes plain pointers and sizes, launches
+ * asynchronously on the caller's CUDA stream (`stream` is a cudaStream_t
+ * passed as void*, NULL = legacy default stream), allocates nothing, and
+ * returns 0 on success or a negative LBM_ERR_* code; lbm_last_error() then
+ * holds a one-line message for the calling thread.
+ *
+ * Reference-facing layout (the arrays the reference's NumPy functions take,
+ * C order): f[nx][ny][9], rho[nx][ny], u[nx][ny][2], all float64, x = axis 0.
+ * D2Q9 directions: c = (0,0),(1,0),(0,1),(-1,0),(0,-1),(1,1),(-1,1),(-1,-1),(1,-1)
+ * (src/lattice_boltzmann_method.py:14-26).
+ *
+ * Resident layout (the hot loop): structure-of-arrays population planes
+ * pop[9][ny][pitch] with x contiguous; the state kept between steps is the
+ * post-collision, pre-streaming population (see lbm_lattice_*).
+ */
+#ifndef LBM_GB300_H
+#define LBM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+#define LBM_OK 0
+#define LBM_ERR_ARG (-1)      /* shape/pointer/argument check failed (reference: AssertionError) */
+#define LBM_ERR_OMEGA (-2)    /* omega outside (0, 2): lattice_boltzmann_method.py:212 */
+#define LBM_ERR_CUDA (-3)     /* a CUDA runtime call failed */
+#define LBM_ERR_UNSUPPORTED (-4)
+
+/* ---- per-node boundary sources ------------------------------------------ */
+/* For every node and direction i the post-streaming population comes from one source:
+ *   PULL   : periodic streaming, f_pre(x - c_i, i)             (np.roll, lattice_boltzmann_method.py:156-157)
+ *   BOUNCE : f_pre(x, opp(i)) - kconst[kset][i]               (rigid_wall :108-109, moving_wall :207-210,
+ *                                                              rigid_object :153-163, boundary_utils.py:179-201)
+ *   CONST  : cconst[cset][i]                                  (inlet :250-251)
+ *   OUTLET : f_prev(x - 1, i), only at column nx-1            (outlet :279-280)
+ * desc bits 2i..2i+1 hold the source of direction i, bits 18..21 kset, 22..25 cset. */
+#define LBM_SRC_PULL 0u
+#define LBM_SRC_BOUNCE 1u
+#define LBM_SRC_CONST 2u
+#define LBM_SRC_OUTLET 3u
+#define LBM_DESC_KSET_SHIFT 18
+#define LBM_DESC_CSET_SHIFT 22
+#define LBM_MAX_SETS 16
+
+typedef struct lbm_geometry {
+  int32_t nx, ny;
+  /* device, [ny][(nx+31)/32] words: bit (x%32) of word x/32 marks a node whose
+   * descriptor is not all-PULL; NULL means every node streams periodically. */
+  const uint32_t* bcmask;
+  /* device, [ny][nx] descriptors (read only where bcmask has the bit set). */
+  const uint32_t* desc;
+  int32_t n_kset, n_cset;
+  double kconst[LBM_MAX_SETS][9]; /* moving-wall terms 2 w_i rho_avg c_i.u_w / c_s^2 (0 = rigid) */
+  double cconst[LBM_MAX_SETS][9]; /* fixed populations (inlet equilibrium) */
+  /* periodic_with_pressure_variations (boundary_conditions.py:286-348): before
+   * streaming, column 0 / column nx-1 directions in pressure_in_dirs /
+   * pressure_out_dirs (bit masks) are rewritten from columns nx-2 / 1. */
+  int32_t pressure;
+  uint32_t pressure_in_dirs, pressure_out_dirs;
+  double rho_in, rho_out;
+  int32_t outlet; /* some node uses LBM_SRC_OUTLET */
+} lbm_geometry;
+
+/* ---- storage / arithmetic of the resident state ------------------------- */
+#define LBM_STORE_F64 0   /* 72 B per node, the drop-in */
+#define LBM_STORE_F32 1   /* 36 B per node */
+#define LBM_STORE_F16S 2  /* 18 B per node, f_i - w_i in binary16 */
+#define LBM_STORE_BF16S 3 /* 18 B per node, f_i - w_i in bfloat16 */
+
+#define LBM_FLAG_EXACT 1  /* float64 arithmetic in the reference's NumPy operation order, no FMA contraction */
+
+/* ---- library ------------------------------------------------------------ */
+int lbm_version(void);
+const char* lbm_last_error(void);
+/* Number of your kernels launched by this thread since the last reset. */
+int64_t lbm_launch_count(int reset);
+
+/* ---- component operators, reference layout, float64 ------------------------ */
+/* compute_density, lattice_boltzmann_method.py:93-105. rho[n] = sum_i f[n][i]. */
+int lbm_density_f64(const double* f, double* rho, int64_t n_nodes, void* stream);
+/* compute_velocity_field, lattice_boltzmann_method.py:108-137 (u = 0 where rho == 0). */
+int lbm_velocity_f64(const double* rho, const double* f, double* u, int64_t n_nodes, void* stream);
+/* equilibrium_distr_func, lattice_boltzmann_method.py:162-188 (any leading shape, flattened). */
+int lbm_equilibrium_f64(const double* rho, const double* u, double* feq, int64_t n_nodes, void* stream);
+/* streaming, lattice_boltzmann_method.py:140-159 (periodic, out of place). */
+int lbm_streaming_f64(const double* f, double* f_out, int32_t nx, int32_t ny, void* stream);
+/* the collision line of lattice_boltzmann_step, lattice_boltzmann_method.py:213-215. */
+int lbm_collide_f64(const double* f, const double* rho, const double* u, double omega,
+                    double* f_pre, int64_t n_nodes, int32_t flags, void* stream);
+/* Applies the BOUNCE / CONST / OUTLET sources of `g` to f_post in place: the
+ * boundary closures rigid_wall, moving_wall, rigid_object, inlet, outlet
+ * (boundary_conditions.py:78-283) compiled into one descriptor. */
+int lbm_apply_boundary_f64(const lbm_geometry* g, const double* f_pre, const double* f_prev,
+                           double* f_post, void* stream);
+/* periodic_with_pressure_variations' closure (boundary_conditions.py:320-346), in place on f_pre. */
+int lbm_pressure_prestream_f64(const lbm_geometry* g, double* f_pre, const double* rho,
+                               const double* u, void* stream);
+/* The single-rank periodic ghost exchange of a ghost-padded (nx+2, ny+2, 9)
+ * array (parallelization_utils.py:23-50 with every neighbour being this rank). */
+int lbm_halo_fill_f64(double* f, int32_t nx_padded, int32_t ny_padded, void* stream);
+
+/* ---- fused step, reference layout ------------------------------------------ */
+/* lattice_boltzmann_step(f, rho, u, omega, boundary) (lattice_boltzmann_method.py:191-228)
+ * with the boundary given as a compiled descriptor `g` (NULL bcmask = no boundary):
+ * collision with the passed-in rho,u, pressure rewrite, streaming, boundary
+ * sources and the moments, in two kernels.  `scratch` must hold
+ * lbm_step_scratch_bytes(nx, ny) bytes (device). */
+size_t lbm_step_scratch_bytes(int32_t nx, int32_t ny);
+int lbm_step_f64(const lbm_geometry* g, const double* f, const double* rho, const double* u,
+                 double omega, double* f_out, double* rho_out, double* u_out, void* scratch,
+                 int32_t flags, void* stream);
+
+/* ---- resident lattice (the hot loop) ----------------------------------------- */
+/* State: pop[9][ny][pitch] (storage type per LBM_STORE_*) holding the
+ * post-collision populations of the last step, plus aux[3][ny] (float64 for
+ * F64 storage, float32 otherwise) holding the pre-collision populations 3,6,7
+ * of column nx-2 that the outlet reads one step later.  pitch must be >= nx
+ * and a multiple of 8. */
+size_t lbm_lattice_pop_bytes(int32_t nx, int32_t ny, int64_t pitch, int32_t storage);
+
+/* First step of a run: collide the reference-layout state (f, and rho,u when
+ * given, else their moments) into pop_out/aux_out. */
+int lbm_lattice_init(const lbm_geometry* g, int32_t storage, const double* f, const double* rho,
+                     const double* u, double omega, void* pop_out, int64_t pitch, void* aux_out,
+                     int32_t flags, void* stream);
+/* nsteps fused pull-stream + boundary + collide steps, ping-ponging between
+ * (pop_a, aux_a) and (pop_b, aux_b), starting from pop_a.  After an odd
+ * number of steps the state is in pop_b.  When rho_out/u_out are not NULL
+ * the moments of the pre-collision state of the LAST step are written as
+ * SoA planes rho[ny][pitch], u[2][ny][pitch] (float64). */
+int lbm_lattice_run(const lbm_geometry* g, int32_t storage, void* pop_a, void* pop_b, int64_t pitch,
+                    void* aux_a, void* aux_b, double omega, int32_t nsteps, double* rho_out,
+                    double* u_out, int32_t flags, void* stream);
+/* Materialise the current (post-streaming, post-boundary) state in the
+ * reference layout: f_out[nx][ny][9], rho_out[nx][ny], u_out[nx][ny][2]
+ * (any may be NULL). */
+int lbm_lattice_read(const lbm_geometry* g, int32_t storage, const void* pop, int64_t pitch,
+                     const void* aux, double* f_out, double* rho_out, double* u_out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBM_GB300_H */

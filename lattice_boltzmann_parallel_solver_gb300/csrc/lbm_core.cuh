@@ -1,0 +1,188 @@
+// lbm_core.cuh -- device building blocks of the D2Q9 BGK hot path (sm_103a).
+//
+// The arithmetic follows src/lattice_boltzmann_method.py of the reference:
+//   rho  = sum_i f_i                                    (:93-105)
+//   u    = (sum_i c_i f_i) / rho, 0 where rho == 0      (:108-137)
+//   feq  = w rho (1 + 3 c.u + 9/2 (c.u)^2 - 3/2 |u|^2)  (:162-188)
+//   fpre = f + (feq - f) omega                          (:215)
+// in two forms: "exact" reproduces NumPy's float64 operation order with no
+// FMA contraction (pairwise 9-term sum, |u|^2 = sqrt(ux^2+uy^2)^2, IEEE
+// division), "fast" regroups the same formula around FMAs and one reciprocal.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/lbm_gb300.h"
+
+namespace lbm {
+
+// D2Q9 velocity set, opposite map and weights (lattice_boltzmann_method.py:14-52).
+__host__ __device__ constexpr int cx(int i) { return (i == 1 || i == 5 || i == 8) ? 1 : ((i == 3 || i == 6 || i == 7) ? -1 : 0); }
+__host__ __device__ constexpr int cy(int i) { return (i == 2 || i == 5 || i == 6) ? 1 : ((i == 4 || i == 7 || i == 8) ? -1 : 0); }
+__host__ __device__ constexpr int opp(int i) { return i == 0 ? 0 : (i <= 4 ? ((i + 1) % 4) + 1 : ((i - 3) % 4) + 5); }
+__host__ __device__ constexpr double wd(int i) { return i == 0 ? 4.0 / 9.0 : (i <= 4 ? 1.0 / 9.0 : 1.0 / 36.0); }
+__host__ __device__ constexpr float wf(int i) { return i == 0 ? 4.0f / 9.0f : (i <= 4 ? 1.0f / 9.0f : 1.0f / 36.0f); }
+static_assert(opp(1) == 3 && opp(2) == 4 && opp(3) == 1 && opp(4) == 2, "opp");
+static_assert(opp(5) == 7 && opp(6) == 8 && opp(7) == 5 && opp(8) == 6, "opp");
+
+// outlet directions (boundary_conditions.py:265) and their slot in aux[3][ny]
+__host__ __device__ constexpr int outlet_slot(int i) { return i == 3 ? 0 : (i == 6 ? 1 : (i == 7 ? 2 : -1)); }
+
+// ---------------------------------------------------------------------------
+// storage of the resident populations
+// ---------------------------------------------------------------------------
+template <int S> struct Store;
+template <> struct Store<LBM_STORE_F64> {
+  using T = double;
+  using R = double;
+  __device__ static R ld(const T* p, int) { return __ldg(p); }
+  __device__ static void st(T* p, R v, int) { *p = v; }
+};
+template <> struct Store<LBM_STORE_F32> {
+  using T = float;
+  using R = float;
+  __device__ static R ld(const T* p, int) { return __ldg(p); }
+  __device__ static void st(T* p, R v, int) { *p = v; }
+};
+// shifted storage: the deviation f_i - w_i is kept in 16 bits
+template <> struct Store<LBM_STORE_F16S> {
+  using T = __half;
+  using R = float;
+  __device__ static R ld(const T* p, int i) { return wf(i) + __half2float(__ldg(p)); }
+  __device__ static void st(T* p, R v, int i) { *p = __float2half_rn(v - wf(i)); }
+};
+template <> struct Store<LBM_STORE_BF16S> {
+  using T = __nv_bfloat16;
+  using R = float;
+  __device__ static R ld(const T* p, int i) { return wf(i) + __bfloat162float(__ldg(p)); }
+  __device__ static void st(T* p, R v, int i) { *p = __float2bfloat16_rn(v - wf(i)); }
+};
+
+// ---------------------------------------------------------------------------
+// moments
+// ---------------------------------------------------------------------------
+// NumPy's float64 reduction of 9 contiguous terms is pairwise:
+// ((f0+f1)+(f2+f3)) + ((f4+f5)+(f6+f7)), then + f8.
+template <typename R>
+__device__ __forceinline__ R density9(const R f[9]) {
+  return (((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7]))) + f[8];
+}
+__device__ __forceinline__ double density9_exact(const double f[9]) {
+  double a = __dadd_rn(__dadd_rn(f[0], f[1]), __dadd_rn(f[2], f[3]));
+  double b = __dadd_rn(__dadd_rn(f[4], f[5]), __dadd_rn(f[6], f[7]));
+  return __dadd_rn(__dadd_rn(a, b), f[8]);
+}
+
+__device__ __forceinline__ void velocity_exact(const double f[9], double rho, double& ux, double& uy) {
+  double jx = __dsub_rn(__dadd_rn(__dadd_rn(f[1], f[5]), f[8]), __dadd_rn(__dadd_rn(f[3], f[6]), f[7]));
+  double jy = __dsub_rn(__dadd_rn(__dadd_rn(f[2], f[5]), f[6]), __dadd_rn(__dadd_rn(f[4], f[7]), f[8]));
+  ux = rho != 0.0 ? __ddiv_rn(jx, rho) : 0.0;
+  uy = rho != 0.0 ? __ddiv_rn(jy, rho) : 0.0;
+}
+
+// Reciprocal by Newton-Raphson iteration r <- r + r (1 - a r) from a
+// single-precision seed; two iterations take the 2^-23 seed error below the
+// float64 rounding error.  Arguments outside the float range fall back to
+// the IEEE division.
+__device__ __forceinline__ double rcp_nr(double a) {
+  float af = __double2float_rn(a);
+  if (!(fabsf(af) > 1e-30f && fabsf(af) < 1e30f)) return 1.0 / a;
+  double r = (double)__frcp_rn(af);
+  double e = fma(-a, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-a, r, 1.0);
+  return fma(r, e, r);
+}
+__device__ __forceinline__ float rcp_nr(float a) { return __frcp_rn(a); }
+
+template <typename R>
+__device__ __forceinline__ void velocity_fast(const R f[9], R rho, R& ux, R& uy) {
+  R jx = ((f[1] + f[5]) + f[8]) - ((f[3] + f[6]) + f[7]);
+  R jy = ((f[2] + f[5]) + f[6]) - ((f[4] + f[7]) + f[8]);
+  R inv = rho != R(0) ? rcp_nr(rho) : R(0);
+  ux = jx * inv;
+  uy = jy * inv;
+}
+
+// ---------------------------------------------------------------------------
+// equilibrium and collision
+// ---------------------------------------------------------------------------
+// c_i.u exactly as the matmul u @ c.T rounds it (one rounding for diagonals)
+__device__ __forceinline__ void cu9_exact(double ux, double uy, double cu[9]) {
+  cu[0] = 0.0;
+  cu[1] = ux;
+  cu[2] = uy;
+  cu[3] = -ux;
+  cu[4] = -uy;
+  cu[5] = __dadd_rn(ux, uy);
+  cu[6] = __dadd_rn(-ux, uy);
+  cu[7] = -cu[5];
+  cu[8] = __dadd_rn(ux, -uy);
+}
+
+// bracket(i) = ((1 + 3 cu) + 4.5 cu^2) - 1.5 |u|^2, |u|^2 = sqrt(ux^2 + uy^2)^2
+__device__ __forceinline__ void bracket9_exact(double ux, double uy, double br[9]) {
+  double nrm = __dsqrt_rn(__dadd_rn(__dmul_rn(ux, ux), __dmul_rn(uy, uy)));
+  double usq15 = __dmul_rn(1.5, __dmul_rn(nrm, nrm));
+  double cu[9];
+  cu9_exact(ux, uy, cu);
+  br[0] = __dsub_rn(1.0, usq15);
+#pragma unroll
+  for (int i = 1; i < 9; ++i)
+    br[i] = __dsub_rn(__dadd_rn(__dadd_rn(1.0, __dmul_rn(3.0, cu[i])), __dmul_rn(4.5, __dmul_rn(cu[i], cu[i]))), usq15);
+}
+
+__device__ __forceinline__ void collide_exact(double f[9], double rho, double ux, double uy, double omega,
+                                              double feq[9], double br[9]) {
+  bracket9_exact(ux, uy, br);
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    feq[i] = __dmul_rn(__dmul_rn(wd(i), rho), br[i]);
+    f[i] = __dadd_rn(f[i], __dmul_rn(__dsub_rn(feq[i], f[i]), omega));
+  }
+}
+
+template <typename R> __device__ constexpr R wr(int i);
+template <> __device__ constexpr double wr<double>(int i) { return wd(i); }
+template <> __device__ constexpr float wr<float>(int i) { return wf(i); }
+
+// Fast form: fpre_i = (1-omega) f_i + omega w_i rho (B + 4.5 cu^2 + 3 cu),
+// B = 1 - 1.5 |u|^2; opposite directions share the even part.
+template <typename R>
+__device__ __forceinline__ void collide_fast(R f[9], R rho, R ux, R uy, R omega) {
+  const R om1 = R(1) - omega;
+  const R usq = fma(ux, ux, uy * uy);
+  const R B = fma(R(-1.5), usq, R(1));
+  const R orho = omega * rho;
+  const R W0 = orho * wr<R>(0), W1 = orho * wr<R>(1), W5 = orho * wr<R>(5);
+  const R V1 = R(3) * W1, V5 = R(3) * W5;
+  f[0] = fma(om1, f[0], W0 * B);
+  const R d58 = ux + uy, d67 = uy - ux;
+#define LBM_PAIR(I, J, V, W, VV)                       \
+  {                                                   \
+    const R t = fma(R(4.5) * (V), (V), B);            \
+    const R s = (W) * t;                              \
+    const R m = (VV) * (V);                           \
+    f[I] = fma(om1, f[I], s + m);                     \
+    f[J] = fma(om1, f[J], s - m);                     \
+  }
+  LBM_PAIR(1, 3, ux, W1, V1)
+  LBM_PAIR(2, 4, uy, W1, V1)
+  LBM_PAIR(5, 7, d58, W5, V5)
+  LBM_PAIR(6, 8, d67, W5, V5)
+#undef LBM_PAIR
+}
+
+// equilibrium with FMAs (used where the fast path needs feq itself)
+template <typename R>
+__device__ __forceinline__ void bracket9_fast(R ux, R uy, R br[9]) {
+  const R B = fma(R(-1.5), fma(ux, ux, uy * uy), R(1));
+  const R cu[9] = {R(0), ux, uy, -ux, -uy, ux + uy, uy - ux, -(ux + uy), ux - uy};
+#pragma unroll
+  for (int i = 0; i < 9; ++i) br[i] = fma(cu[i], fma(R(4.5), cu[i], R(3)), B);
+}
+
+}  // namespace lbm

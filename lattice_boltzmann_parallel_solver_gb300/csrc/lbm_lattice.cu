@@ -1,0 +1,415 @@
+// lbm_lattice.cu -- fused pull-scheme stream + boundary + collide kernel and
+// the C ABI of the drop-in step and of the resident lattice.
+//
+// State convention.  The reference's step (lattice_boltzmann_method.py:191-228)
+// maps the post-streaming state f_n to f_{n+1} = BC(stream(collide(f_n))).
+// The resident state kept here is S_n = collide(f_n) with the pre-streaming
+// pressure rewrite already applied (boundary_conditions.py:320-346), so one
+// kernel per step reads S_{n-1} once (pull: node x takes S(x - c_i, i)),
+// applies the boundary sources, forms the moments of f_n, collides and
+// writes S_n once: 72 B read + 72 B written per node in float64.
+//   MODE_INIT  : S_0 = collide(f_0) from a reference-layout f_0 (rho,u passed in or recomputed)
+//   MODE_FUSED : S_n from S_{n-1}
+//   MODE_READ  : f_n = BC(stream(S_{n-1})) and its moments, in the reference layout
+// The outlet (boundary_conditions.py:279-280) needs f_{n-1} at column nx-2;
+// each kernel stores those three populations in aux[3][ny] for the next one.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+
+#include "lbm_core.cuh"
+#include "lbm_host.h"
+
+namespace lbm {
+
+enum { MODE_INIT = 0, MODE_FUSED = 1, MODE_READ = 2 };
+
+struct GeoK {
+  int nx, ny, words;
+  const uint32_t* bcmask;
+  const uint32_t* desc;
+  int pressure;
+  uint32_t pin, pout;
+  double rho_in, rho_out;
+  int outlet;
+  double kconst[LBM_MAX_SETS][9];
+  double cconst[LBM_MAX_SETS][9];
+};
+
+struct View {
+  const double* p;
+  int64_t sx, sy, sc;
+};
+struct OutView {
+  double* p;
+  int64_t sx, sy, sc;
+};
+
+struct KParams {
+  GeoK g;
+  const void* pop_in;
+  void* pop_out;
+  int64_t pitch, plane;
+  const void* aux_in;
+  void* aux_out;
+  View f_in, rho_in, u_in;
+  OutView f_out, rho_out, u_out;
+  double omega;
+};
+
+template <int STORE, bool EXACT, int MODE>
+__global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KParams P) {
+  using St = Store<STORE>;
+  using T = typename St::T;
+  using R = typename St::R;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  const int nx = P.g.nx, ny = P.g.ny;
+  if (x >= nx || y >= ny) return;
+  const int64_t r0 = (int64_t)y * P.pitch;
+  const R* aux_in = static_cast<const R*>(P.aux_in);
+
+  R f[9];
+  if (MODE == MODE_INIT) {
+    const double* src = P.f_in.p + x * P.f_in.sx + y * P.f_in.sy;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) f[i] = (R)src[i * P.f_in.sc];
+  } else {
+    // pull: direction i arrives from node (x - cx_i, y - cy_i), periodic
+    const int xm = x == 0 ? nx - 1 : x - 1, xp = x == nx - 1 ? 0 : x + 1;
+    const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
+    const int64_t rm = (int64_t)ym * P.pitch, rp = (int64_t)yp * P.pitch;
+    const T* pin = static_cast<const T*>(P.pop_in);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      const int xs = cx(i) == 1 ? xm : (cx(i) == -1 ? xp : x);
+      const int64_t rs = cy(i) == 1 ? rm : (cy(i) == -1 ? rp : r0);
+      f[i] = St::ld(pin + i * P.plane + rs + xs, i);
+    }
+    if (P.g.bcmask != nullptr) {
+      const uint32_t word = __ldg(P.g.bcmask + (int64_t)y * P.g.words + (x >> 5));
+      if ((word >> (x & 31)) & 1u) {
+        const uint32_t d = __ldg(P.g.desc + (int64_t)y * nx + x);
+        const int ks = (d >> LBM_DESC_KSET_SHIFT) & 15, cs = (d >> LBM_DESC_CSET_SHIFT) & 15;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+          const uint32_t s = (d >> (2 * i)) & 3u;
+          if (s == LBM_SRC_BOUNCE) {
+            const R v = St::ld(pin + opp(i) * P.plane + r0 + x, opp(i));
+            if (EXACT)
+              f[i] = (R)__dsub_rn((double)v, P.g.kconst[ks][i]);
+            else
+              f[i] = v - (R)P.g.kconst[ks][i];
+          } else if (s == LBM_SRC_CONST) {
+            f[i] = (R)P.g.cconst[cs][i];
+          } else if (s == LBM_SRC_OUTLET && outlet_slot(i) >= 0 && aux_in != nullptr) {
+            f[i] = aux_in[outlet_slot(i) * ny + y];
+          }
+        }
+      }
+    }
+  }
+
+  // outlet memory: the pre-collision populations 3,6,7 of column nx-2
+  if (MODE != MODE_READ && P.aux_out != nullptr && x == nx - 2) {
+    R* aux_out = static_cast<R*>(P.aux_out);
+    aux_out[0 * ny + y] = f[3];
+    aux_out[1 * ny + y] = f[6];
+    aux_out[2 * ny + y] = f[7];
+  }
+
+  // moments of f_n; the collision of the first step uses the rho,u passed in
+  R rho, ux, uy;
+  const bool given = MODE == MODE_INIT && P.rho_in.p != nullptr;
+  if (given) {
+    rho = (R)P.rho_in.p[x * P.rho_in.sx + y * P.rho_in.sy];
+    const double* up = P.u_in.p + x * P.u_in.sx + y * P.u_in.sy;
+    ux = (R)up[0];
+    uy = (R)up[P.u_in.sc];
+  } else if (EXACT || MODE == MODE_READ) {
+    // read-out moments always follow compute_density / compute_velocity_field exactly
+    double fd[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) fd[i] = (double)f[i];
+    const double r = density9_exact(fd);
+    double a, b;
+    velocity_exact(fd, r, a, b);
+    rho = (R)r;
+    ux = (R)a;
+    uy = (R)b;
+  } else {
+    rho = density9(f);
+    velocity_fast(f, rho, ux, uy);
+  }
+
+  if (MODE == MODE_READ || (MODE == MODE_FUSED && P.rho_out.p != nullptr)) {
+    if (P.rho_out.p != nullptr) P.rho_out.p[x * P.rho_out.sx + y * P.rho_out.sy] = (double)rho;
+    if (P.u_out.p != nullptr) {
+      double* up = P.u_out.p + x * P.u_out.sx + y * P.u_out.sy;
+      up[0] = (double)ux;
+      up[P.u_out.sc] = (double)uy;
+    }
+  }
+  if (MODE == MODE_READ) {
+    if (P.f_out.p != nullptr) {
+      double* dst = P.f_out.p + x * P.f_out.sx + y * P.f_out.sy;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) dst[i * P.f_out.sc] = (double)f[i];
+    }
+    return;
+  }
+
+  // collision
+  const bool pressure_src = P.g.pressure && (x == nx - 2 || x == 1);
+  R pin_v[9], pout_v[9];
+  if (EXACT) {
+    double fd[9], feq[9], br[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) fd[i] = (double)f[i];
+    collide_exact(fd, (double)rho, (double)ux, (double)uy, P.omega, feq, br);
+    if (pressure_src) {
+      // feq(rho_in, u(nx-2)) + (fpre - feq(rho, u))  at column 0, and the outlet analogue
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        const double neq = __dsub_rn(fd[i], feq[i]);
+        pin_v[i] = (R)__dadd_rn(__dmul_rn(__dmul_rn(wd(i), P.g.rho_in), br[i]), neq);
+        pout_v[i] = (R)__dadd_rn(__dmul_rn(__dmul_rn(wd(i), P.g.rho_out), br[i]), neq);
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) f[i] = (R)fd[i];
+  } else {
+    collide_fast(f, rho, ux, uy, (R)P.omega);
+    if (pressure_src) {
+      R br[9];
+      bracket9_fast(ux, uy, br);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        pin_v[i] = fma(wr<R>(i) * br[i], (R)P.g.rho_in - rho, f[i]);
+        pout_v[i] = fma(wr<R>(i) * br[i], (R)P.g.rho_out - rho, f[i]);
+      }
+    }
+  }
+
+  // store S_n; columns 0 / nx-1 take the pressure rewrite from columns nx-2 / 1
+  T* pout = static_cast<T*>(P.pop_out);
+  const uint32_t skip = P.g.pressure ? ((x == 0 ? P.g.pin : 0u) | (x == nx - 1 ? P.g.pout : 0u)) : 0u;
+#pragma unroll
+  for (int i = 0; i < 9; ++i)
+    if (!((skip >> i) & 1u)) St::st(pout + i * P.plane + r0 + x, f[i], i);
+  if (pressure_src) {
+    if (x == nx - 2) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i)
+        if ((P.g.pin >> i) & 1u) St::st(pout + i * P.plane + r0 + 0, pin_v[i], i);
+    }
+    if (x == 1) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i)
+        if ((P.g.pout >> i) & 1u) St::st(pout + i * P.plane + r0 + (nx - 1), pout_v[i], i);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static bool to_geok(const lbm_geometry* g, GeoK& k) {
+  if (g == nullptr) return set_error(LBM_ERR_ARG, "geometry is NULL"), false;
+  if (g->nx < 1 || g->ny < 1) return set_error(LBM_ERR_ARG, "nx and ny must be >= 1"), false;
+  if (g->bcmask != nullptr && g->desc == nullptr)
+    return set_error(LBM_ERR_ARG, "bcmask given without desc"), false;
+  if (g->n_kset < 0 || g->n_kset > LBM_MAX_SETS || g->n_cset < 0 || g->n_cset > LBM_MAX_SETS)
+    return set_error(LBM_ERR_ARG, "constant-set count out of range"), false;
+  if (g->pressure && g->nx < 2)
+    return set_error(LBM_ERR_ARG, "the pressure rewrite needs nx >= 2"), false;
+  if (g->outlet && g->nx < 2) return set_error(LBM_ERR_ARG, "the outlet needs nx >= 2"), false;
+  std::memset(&k, 0, sizeof(k));
+  k.nx = g->nx;
+  k.ny = g->ny;
+  k.words = (g->nx + 31) / 32;
+  k.bcmask = g->bcmask;
+  k.desc = g->desc;
+  k.pressure = g->pressure;
+  k.pin = g->pressure_in_dirs & 0x1FFu;
+  k.pout = g->pressure_out_dirs & 0x1FFu;
+  k.rho_in = g->rho_in;
+  k.rho_out = g->rho_out;
+  k.outlet = g->outlet;
+  std::memcpy(k.kconst, g->kconst, sizeof(k.kconst));
+  std::memcpy(k.cconst, g->cconst, sizeof(k.cconst));
+  return true;
+}
+
+static void launch_dims(int nx, int ny, dim3& grid, dim3& block) {
+  int bx = nx >= 128 ? 128 : ((nx + 31) / 32) * 32;
+  int by = std::max(1, 128 / bx);
+  block = dim3(bx, by, 1);
+  grid = dim3((nx + bx - 1) / bx, (ny + by - 1) / by, 1);
+}
+
+template <int STORE, bool EXACT, int MODE>
+static int launch(const KParams& P, cudaStream_t s) {
+  dim3 grid, block;
+  launch_dims(P.g.nx, P.g.ny, grid, block);
+  lattice_kernel<STORE, EXACT, MODE><<<grid, block, 0, s>>>(P);
+  count_launch();
+  return check_launch("lattice_kernel");
+}
+
+template <int MODE>
+static int dispatch(int storage, bool exact, const KParams& P, cudaStream_t s) {
+  if (exact && storage != LBM_STORE_F64)
+    return set_error(LBM_ERR_UNSUPPORTED, "exact arithmetic needs float64 storage");
+  switch (storage) {
+    case LBM_STORE_F64:
+      return exact ? launch<LBM_STORE_F64, true, MODE>(P, s) : launch<LBM_STORE_F64, false, MODE>(P, s);
+    case LBM_STORE_F32: return launch<LBM_STORE_F32, false, MODE>(P, s);
+    case LBM_STORE_F16S: return launch<LBM_STORE_F16S, false, MODE>(P, s);
+    case LBM_STORE_BF16S: return launch<LBM_STORE_BF16S, false, MODE>(P, s);
+    default: return set_error(LBM_ERR_ARG, "unknown storage type");
+  }
+}
+
+static size_t store_bytes(int storage) {
+  switch (storage) {
+    case LBM_STORE_F64: return 8;
+    case LBM_STORE_F32: return 4;
+    case LBM_STORE_F16S:
+    case LBM_STORE_BF16S: return 2;
+    default: return 0;
+  }
+}
+
+static View ref_f(const double* p, int ny) { return View{p, 9LL * ny, 9, 1}; }
+static View ref_rho(const double* p, int ny) { return View{p, (int64_t)ny, 1, 0}; }
+static View ref_u(const double* p, int ny) { return View{p, 2LL * ny, 2, 1}; }
+static OutView ref_f_out(double* p, int ny) { return OutView{p, 9LL * ny, 9, 1}; }
+static OutView ref_rho_out(double* p, int ny) { return OutView{p, (int64_t)ny, 1, 0}; }
+static OutView ref_u_out(double* p, int ny) { return OutView{p, 2LL * ny, 2, 1}; }
+
+static int check_omega(double omega) {
+  if (!(omega > 0.0 && omega < 2.0)) return set_error(LBM_ERR_OMEGA, "omega must lie in (0, 2)");
+  return LBM_OK;
+}
+
+static int check_pitch(int nx, int64_t pitch) {
+  if (pitch < nx || pitch % 8 != 0) return set_error(LBM_ERR_ARG, "pitch must be >= nx and a multiple of 8");
+  return LBM_OK;
+}
+
+}  // namespace lbm
+
+using namespace lbm;
+
+extern "C" {
+
+size_t lbm_lattice_pop_bytes(int32_t nx, int32_t ny, int64_t pitch, int32_t storage) {
+  (void)nx;
+  return (size_t)9 * (size_t)ny * (size_t)pitch * store_bytes(storage);
+}
+
+int lbm_lattice_init(const lbm_geometry* g, int32_t storage, const double* f, const double* rho,
+                     const double* u, double omega, void* pop_out, int64_t pitch, void* aux_out,
+                     int32_t flags, void* stream) {
+  KParams P;
+  std::memset(&P, 0, sizeof(P));
+  if (!to_geok(g, P.g)) return last_status();
+  if (int e = check_omega(omega)) return e;
+  if (int e = check_pitch(g->nx, pitch)) return e;
+  if (f == nullptr || pop_out == nullptr) return set_error(LBM_ERR_ARG, "f and pop_out are required");
+  if ((rho == nullptr) != (u == nullptr)) return set_error(LBM_ERR_ARG, "rho and u must be given together");
+  if (g->outlet && aux_out == nullptr) return set_error(LBM_ERR_ARG, "the outlet needs aux_out");
+  P.pop_out = pop_out;
+  P.pitch = pitch;
+  P.plane = pitch * g->ny;
+  P.aux_out = aux_out;
+  P.f_in = ref_f(f, g->ny);
+  if (rho) {
+    P.rho_in = ref_rho(rho, g->ny);
+    P.u_in = ref_u(u, g->ny);
+  }
+  P.omega = omega;
+  return dispatch<MODE_INIT>(storage, flags & LBM_FLAG_EXACT, P, (cudaStream_t)stream);
+}
+
+int lbm_lattice_run(const lbm_geometry* g, int32_t storage, void* pop_a, void* pop_b, int64_t pitch,
+                    void* aux_a, void* aux_b, double omega, int32_t nsteps, double* rho_out,
+                    double* u_out, int32_t flags, void* stream) {
+  KParams P;
+  std::memset(&P, 0, sizeof(P));
+  if (!to_geok(g, P.g)) return last_status();
+  if (int e = check_omega(omega)) return e;
+  if (int e = check_pitch(g->nx, pitch)) return e;
+  if (pop_a == nullptr || pop_b == nullptr || pop_a == pop_b)
+    return set_error(LBM_ERR_ARG, "two distinct population buffers are required");
+  if (g->outlet && (aux_a == nullptr || aux_b == nullptr || aux_a == aux_b))
+    return set_error(LBM_ERR_ARG, "the outlet needs two distinct aux buffers");
+  if (nsteps < 0) return set_error(LBM_ERR_ARG, "nsteps must be >= 0");
+  P.pitch = pitch;
+  P.plane = pitch * g->ny;
+  P.omega = omega;
+  for (int s = 0; s < nsteps; ++s) {
+    const bool even = (s % 2) == 0;
+    P.pop_in = even ? pop_a : pop_b;
+    P.pop_out = even ? pop_b : pop_a;
+    P.aux_in = even ? aux_a : aux_b;
+    P.aux_out = even ? aux_b : aux_a;
+    const bool last = s == nsteps - 1;
+    P.rho_out = OutView{last ? rho_out : nullptr, 1, pitch, 0};
+    P.u_out = OutView{last ? u_out : nullptr, 1, pitch, pitch * g->ny};
+    if (int e = dispatch<MODE_FUSED>(storage, flags & LBM_FLAG_EXACT, P, (cudaStream_t)stream)) return e;
+  }
+  return LBM_OK;
+}
+
+int lbm_lattice_read(const lbm_geometry* g, int32_t storage, const void* pop, int64_t pitch, const void* aux,
+                     double* f_out, double* rho_out, double* u_out, void* stream) {
+  KParams P;
+  std::memset(&P, 0, sizeof(P));
+  if (!to_geok(g, P.g)) return last_status();
+  if (int e = check_pitch(g->nx, pitch)) return e;
+  if (pop == nullptr) return set_error(LBM_ERR_ARG, "pop is required");
+  if (g->outlet && aux == nullptr) return set_error(LBM_ERR_ARG, "the outlet needs aux");
+  P.pop_in = pop;
+  P.aux_in = aux;
+  P.pitch = pitch;
+  P.plane = pitch * g->ny;
+  P.f_out = ref_f_out(f_out, g->ny);
+  P.rho_out = ref_rho_out(rho_out, g->ny);
+  P.u_out = ref_u_out(u_out, g->ny);
+  return dispatch<MODE_READ>(storage, false, P, (cudaStream_t)stream);
+}
+
+size_t lbm_step_scratch_bytes(int32_t nx, int32_t ny) {
+  const int64_t pitch = ((int64_t)nx + 31) / 32 * 32;
+  return (size_t)(9 * pitch * ny + 3 * (int64_t)ny) * sizeof(double) + 256;
+}
+
+int lbm_step_f64(const lbm_geometry* g, const double* f, const double* rho, const double* u, double omega,
+                 double* f_out, double* rho_out, double* u_out, void* scratch, int32_t flags, void* stream) {
+  if (g == nullptr) return set_error(LBM_ERR_ARG, "geometry is NULL");
+  if (f == nullptr || rho == nullptr || u == nullptr || f_out == nullptr || rho_out == nullptr ||
+      u_out == nullptr || scratch == nullptr)
+    return set_error(LBM_ERR_ARG, "f, rho, u, f_out, rho_out, u_out and scratch are required");
+  const int64_t pitch = ((int64_t)g->nx + 31) / 32 * 32;
+  uintptr_t base = ((uintptr_t)scratch + 255) & ~(uintptr_t)255;
+  double* pop = reinterpret_cast<double*>(base);
+  double* aux = pop + 9 * pitch * g->ny;
+  if (int e = lbm_lattice_init(g, LBM_STORE_F64, f, rho, u, omega, pop, pitch, aux, flags, stream)) return e;
+  // the read-out kernel recomputes the moments the same way in both forms
+  KParams P;
+  std::memset(&P, 0, sizeof(P));
+  if (!to_geok(g, P.g)) return last_status();
+  P.pop_in = pop;
+  P.aux_in = aux;
+  P.pitch = pitch;
+  P.plane = pitch * g->ny;
+  P.f_out = ref_f_out(f_out, g->ny);
+  P.rho_out = ref_rho_out(rho_out, g->ny);
+  P.u_out = ref_u_out(u_out, g->ny);
+  return (flags & LBM_FLAG_EXACT) ? launch<LBM_STORE_F64, true, MODE_READ>(P, (cudaStream_t)stream)
+                                  : launch<LBM_STORE_F64, false, MODE_READ>(P, (cudaStream_t)stream);
+}
+
+}  // extern "C"

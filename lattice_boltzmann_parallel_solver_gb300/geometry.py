@@ -1,0 +1,114 @@
+"""Boundary compiler: the reference's boundary closures, applied in order,
+turned into one per-node descriptor the CUDA kernels read.
+
+For every node and direction the post-streaming population has exactly one
+source, set by the LAST closure that writes it (the reference applies its
+closures one after another, boundary_utils.py:51-52, 103-106, 165-201, and
+every closure reads f_pre, f_prev or a constant, never another closure's
+output):
+
+  PULL    periodic streaming                      (lattice_boltzmann_method.py:156-157)
+  BOUNCE  f_pre(x, opp i) - k                     (boundary_conditions.py:108-109, 156, 162, 207-210)
+  CONST   a fixed population                      (boundary_conditions.py:250-251)
+  OUTLET  f_prev(x - 1, i)                        (boundary_conditions.py:279-280)
+
+The descriptor is a uint32 per node ([ny][nx], x fastest) plus a bit mask
+[ny][ceil(nx/32)] marking the nodes that have one; the constants k and the
+fixed populations go into two small tables passed by value to the kernels.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+
+PULL, BOUNCE, CONST, OUTLET = _lib.SRC_PULL, _lib.SRC_BOUNCE, _lib.SRC_CONST, _lib.SRC_OUTLET
+
+
+def dir_mask(dirs) -> int:
+    m = 0
+    for i in dirs:
+        m |= 1 << int(i)
+    return m
+
+
+class CompiledGeometry:
+    """Device-resident descriptor of one boundary composition on an nx x ny lattice."""
+
+    def __init__(self, nx: int, ny: int, sources=(), pressure=None, device="cuda"):
+        self.nx, self.ny = int(nx), int(ny)
+        src = np.zeros((nx, ny, 9), dtype=np.uint32)
+        kv = np.zeros((nx, ny, 9))
+        cv = np.zeros((nx, ny, 9))
+        for mask, i, kind, value in sources:
+            mask = np.asarray(mask, dtype=bool)
+            assert mask.shape == (nx, ny), "boundary mask shape %s does not match the lattice %s" % (
+                mask.shape, (nx, ny))
+            src[mask, i] = kind
+            kv[mask, i] = value if kind == BOUNCE else 0.0
+            cv[mask, i] = value if kind == CONST else 0.0
+        special = (src != PULL).any(axis=-1)
+        self.n_special = int(special.sum())
+        outlet_cols = np.nonzero((src == OUTLET).any(axis=(1, 2)))[0]
+        self.outlet = bool(outlet_cols.size)
+        # the fused kernels keep the outlet's previous populations for column nx-1 only
+        self.fusable = bool(np.all(outlet_cols == nx - 1))
+
+        g = _lib.Geometry()
+        g.nx, g.ny = self.nx, self.ny
+        g.outlet = int(self.outlet)
+        if self.n_special:
+            ktab, kidx = np.unique(kv[special], axis=0, return_inverse=True)
+            ctab, cidx = np.unique(cv[special], axis=0, return_inverse=True)
+            if len(ktab) > _lib.MAX_SETS or len(ctab) > _lib.MAX_SETS:
+                raise NotImplementedError("more than %d distinct boundary constant sets" % _lib.MAX_SETS)
+            desc = np.zeros((nx, ny), dtype=np.uint32)
+            for i in range(9):
+                desc |= src[..., i] << np.uint32(2 * i)
+            desc[special] |= (kidx.reshape(-1).astype(np.uint32) << np.uint32(_lib.KSET_SHIFT)) | \
+                (cidx.reshape(-1).astype(np.uint32) << np.uint32(_lib.CSET_SHIFT))
+            words = (nx + 31) // 32
+            bits = np.zeros((ny, words * 32), dtype=np.uint64)
+            bits[:, :nx] = special.T
+            bits = bits.reshape(ny, words, 32)
+            bcmask = (bits << np.arange(32, dtype=np.uint64)).sum(axis=-1).astype(np.uint32)
+            self.desc = torch.from_numpy(np.ascontiguousarray(desc.T)).to(device)
+            self.bcmask = torch.from_numpy(np.ascontiguousarray(bcmask)).to(device)
+            g.desc = self.desc.data_ptr()
+            g.bcmask = self.bcmask.data_ptr()
+            g.n_kset, g.n_cset = len(ktab), len(ctab)
+            for s in range(len(ktab)):
+                for i in range(9):
+                    g.kconst[s][i] = float(ktab[s, i])
+            for s in range(len(ctab)):
+                for i in range(9):
+                    g.cconst[s][i] = float(ctab[s, i])
+        else:
+            self.desc = self.bcmask = None
+        if pressure is not None:
+            pin, pout, rho_in, rho_out = pressure
+            g.pressure = 1
+            g.pressure_in_dirs = dir_mask(pin)
+            g.pressure_out_dirs = dir_mask(pout)
+            g.rho_in, g.rho_out = float(rho_in), float(rho_out)
+            assert nx >= 2
+        self.pressure = pressure
+        self.struct = g
+
+    @property
+    def ref(self):
+        return ctypes.byref(self.struct)
+
+
+_EMPTY = {}
+
+
+def empty_geometry(nx: int, ny: int) -> CompiledGeometry:
+    """Fully periodic lattice: every node streams."""
+    key = (int(nx), int(ny))
+    if key not in _EMPTY:
+        _EMPTY[key] = CompiledGeometry(nx, ny)
+    return _EMPTY[key]

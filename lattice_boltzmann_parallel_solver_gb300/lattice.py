@@ -1,0 +1,160 @@
+"""Device-resident lattice: the hot loop of the reference's drivers
+(for example experiments.py:83-84, 324-325, 766-767) without host round trips.
+
+The populations live on the device as structure-of-arrays planes
+pop[9][ny][pitch] (x contiguous, pitch a multiple of 32 elements) in one of
+four storage forms:
+
+  "f64"   float64 storage and arithmetic: the drop-in (72 B per node)
+  "f32"   float32 storage and arithmetic (36 B)
+  "f16"   float32 arithmetic, f_i - w_i stored in binary16 (18 B)
+  "bf16"  float32 arithmetic, f_i - w_i stored in bfloat16 (18 B)
+
+One fused kernel per step reads the previous post-collision populations
+once, streams them by pulling, applies the boundary descriptor, forms the
+moments, collides and writes the new post-collision populations once.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _arrays as A
+from . import _lib
+from .geometry import empty_geometry
+
+STORAGES = {
+    "f64": (_lib.STORE_F64, torch.float64, torch.float64),
+    "f32": (_lib.STORE_F32, torch.float32, torch.float32),
+    "f16": (_lib.STORE_F16S, torch.float16, torch.float32),
+    "bf16": (_lib.STORE_BF16S, torch.bfloat16, torch.float32),
+}
+BYTES_PER_NODE = {"f64": 144, "f32": 72, "f16": 36, "bf16": 36}
+
+
+class Lattice:
+    """An nx x ny D2Q9 lattice with a fused boundary composition, resident on the device."""
+
+    def __init__(self, nx: int, ny: int, omega: float, boundary=None, storage: str = "f64",
+                 exact: bool = False, device: str = "cuda"):
+        A.require_cuda()
+        assert 0 < omega < 2
+        assert storage in STORAGES, "storage must be one of %s" % sorted(STORAGES)
+        assert not (exact and storage != "f64"), "exact arithmetic needs float64 storage"
+        self.nx, self.ny, self.omega = int(nx), int(ny), float(omega)
+        self.storage = storage
+        self.store_id, self.pop_dtype, self.aux_dtype = STORAGES[storage]
+        self.flags = _lib.FLAG_EXACT if exact else 0
+        self.pitch = (self.nx + 31) // 32 * 32
+        self.device = torch.device(device)
+        self.boundary = boundary
+        self.geo = boundary.geometry(self.nx, self.ny) if boundary is not None else empty_geometry(self.nx, self.ny)
+        if not self.geo.fusable:
+            raise NotImplementedError("the outlet must sit on column nx-1 for the resident lattice")
+        n = 9 * self.ny * self.pitch
+        self.pop = [torch.empty(n, dtype=self.pop_dtype, device=self.device) for _ in range(2)]
+        self.aux = [torch.zeros(3 * self.ny, dtype=self.aux_dtype, device=self.device) for _ in range(2)]
+        self.cur = 0
+        self.t = 0
+        self._init = None
+        self._graphs = {}
+
+    # -- state ------------------------------------------------------------------
+    def set_state(self, f, density=None, velocity=None):
+        """Start from a reference-layout state f[nx, ny, 9]; the first step's
+        collision uses ``density``/``velocity`` when given (as the reference's
+        step does), else their moments."""
+        f = A.to_device(f)
+        assert tuple(f.shape) == (self.nx, self.ny, 9)
+        rho = A.to_device(density) if density is not None else None
+        u = A.to_device(velocity) if velocity is not None else None
+        if rho is not None:
+            assert tuple(rho.shape) == (self.nx, self.ny) and tuple(u.shape) == (self.nx, self.ny, 2)
+        self._init = (f.clone(), None if rho is None else rho.clone(), None if u is None else u.clone())
+        self.t = 0
+        self.cur = 0
+        self._graphs.clear()
+        return self
+
+    @property
+    def state_bytes(self) -> int:
+        return sum(t.numel() * t.element_size() for t in self.pop + self.aux)
+
+    # -- stepping ---------------------------------------------------------------
+    def _first(self):
+        f, rho, u = self._init
+        _lib.call("lbm_lattice_init", self.geo.ref, self.store_id, f.data_ptr(), A.ptr(rho), A.ptr(u),
+                  self.omega, self.pop[self.cur].data_ptr(), self.pitch, self.aux[self.cur].data_ptr(),
+                  self.flags, A.stream())
+        self._init = None
+        self.t += 1
+
+    def _run(self, n: int, rho_out=None, u_out=None):
+        a, b = self.cur, 1 - self.cur
+        _lib.call("lbm_lattice_run", self.geo.ref, self.store_id, self.pop[a].data_ptr(), self.pop[b].data_ptr(),
+                  self.pitch, self.aux[a].data_ptr(), self.aux[b].data_ptr(), self.omega, int(n),
+                  A.ptr(rho_out), A.ptr(u_out), self.flags, A.stream())
+        if n % 2:
+            self.cur = b
+        self.t += n
+
+    def step(self, n: int = 1):
+        """Advance n time steps (asynchronous on the current stream)."""
+        if n <= 0:
+            return self
+        if self._init is not None:
+            self._first()
+            n -= 1
+        if n > 0:
+            self._run(n)
+        return self
+
+    def step_graph(self, n: int, chunk: int = 64):
+        """Advance n steps replaying a captured CUDA graph of ``chunk`` fused
+        steps (chunk even, so the buffers return to their places); for small
+        lattices where launch latency would dominate."""
+        assert chunk % 2 == 0 and chunk > 0
+        if self._init is not None:
+            self._first()
+            n -= 1
+        full, rest = divmod(max(n, 0), chunk)
+        if full:
+            key = (chunk, self.cur)
+            g = self._graphs.get(key)
+            if g is None:
+                g = torch.cuda.CUDAGraph()
+                side = torch.cuda.Stream()
+                side.wait_stream(torch.cuda.current_stream())
+                with torch.cuda.stream(side):
+                    with torch.cuda.graph(g, stream=side):
+                        _lib.call("lbm_lattice_run", self.geo.ref, self.store_id, self.pop[self.cur].data_ptr(),
+                                  self.pop[1 - self.cur].data_ptr(), self.pitch, self.aux[self.cur].data_ptr(),
+                                  self.aux[1 - self.cur].data_ptr(), self.omega, chunk, 0, 0, self.flags,
+                                  side.cuda_stream)
+                torch.cuda.current_stream().wait_stream(side)
+                self._graphs[key] = g
+            for _ in range(full):
+                g.replay()
+            self.t += full * chunk
+        if rest:
+            self._run(rest)
+        return self
+
+    # -- read-out ---------------------------------------------------------------
+    def read(self, want_f: bool = True):
+        """(f[nx, ny, 9], rho[nx, ny], u[nx, ny, 2]) of the current state, float64,
+        reference layout, on the device."""
+        if self._init is not None:
+            f, rho, u = self._init
+            from .lattice_boltzmann_method import compute_density, compute_velocity_field
+            r = compute_density(f)
+            return (f.clone() if want_f else None), r, compute_velocity_field(r, f)
+        f = torch.empty((self.nx, self.ny, 9), dtype=torch.float64, device=self.device) if want_f else None
+        rho = torch.empty((self.nx, self.ny), dtype=torch.float64, device=self.device)
+        u = torch.empty((self.nx, self.ny, 2), dtype=torch.float64, device=self.device)
+        _lib.call("lbm_lattice_read", self.geo.ref, self.store_id, self.pop[self.cur].data_ptr(), self.pitch,
+                  self.aux[self.cur].data_ptr(), A.ptr(f), rho.data_ptr(), u.data_ptr(), A.stream())
+        return f, rho, u
+
+    def moments(self):
+        _, rho, u = self.read(want_f=False)
+        return rho, u
