@@ -170,7 +170,7 @@ def test_density_wave_fit_matches_oracle(pkg):
         assert abs(np.abs(r - 1).max() - np.abs(ro - 1).max()) <= 1e-13
 
 
-@pytest.mark.parametrize("storage,tol", [("f32", 1e-5), ("f16", 1e-3), ("bf16", 1e-2)])
+@pytest.mark.parametrize("storage,tol", [("f32", 1e-4), ("f16", 1e-3), ("bf16", 1e-2)])
 def test_reduced_precision_velocity_error(pkg, storage, tol):
     """Relative velocity L2 error of the reduced-precision storages against the
     float64 oracle on the 128^2 cavity after 1000 steps (stated tolerances)."""
