@@ -75,6 +75,8 @@ typedef struct lbm_geometry {
 #define LBM_STORE_BF16S 3 /* 18 B per node, f_i - w_i in bfloat16 */
 
 #define LBM_FLAG_EXACT 1  /* float64 arithmetic in the reference's NumPy operation order, no FMA contraction */
+#define LBM_FLAG_GENERIC 2 /* use the one-node-per-thread kernel instead of the vectorised one */
+#define LBM_FLAG_NPT_SHIFT 4 /* bits 4..7: nodes per thread of the vectorised kernel (0 = default) */
 
 /* ---- library ------------------------------------------------------------ */
 int lbm_version(void);

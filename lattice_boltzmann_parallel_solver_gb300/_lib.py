@@ -23,6 +23,8 @@ MAX_SETS = 16
 
 STORE_F64, STORE_F32, STORE_F16S, STORE_BF16S = 0, 1, 2, 3
 FLAG_EXACT = 1
+FLAG_GENERIC = 2
+FLAG_NPT_SHIFT = 4
 
 vp = C.c_void_p
 i32 = C.c_int32

@@ -40,12 +40,16 @@ template <> struct Store<LBM_STORE_F64> {
   using R = double;
   __device__ static R ld(const T* p, int) { return __ldg(p); }
   __device__ static void st(T* p, R v, int) { *p = v; }
+  __device__ static R to_r(T t, int) { return t; }
+  __device__ static T from_r(R v, int) { return v; }
 };
 template <> struct Store<LBM_STORE_F32> {
   using T = float;
   using R = float;
   __device__ static R ld(const T* p, int) { return __ldg(p); }
   __device__ static void st(T* p, R v, int) { *p = v; }
+  __device__ static R to_r(T t, int) { return t; }
+  __device__ static T from_r(R v, int) { return v; }
 };
 // shifted storage: the deviation f_i - w_i is kept in 16 bits
 template <> struct Store<LBM_STORE_F16S> {
@@ -53,13 +57,62 @@ template <> struct Store<LBM_STORE_F16S> {
   using R = float;
   __device__ static R ld(const T* p, int i) { return wf(i) + __half2float(__ldg(p)); }
   __device__ static void st(T* p, R v, int i) { *p = __float2half_rn(v - wf(i)); }
+  __device__ static R to_r(T t, int i) { return wf(i) + __half2float(t); }
+  __device__ static T from_r(R v, int i) { return __float2half_rn(v - wf(i)); }
 };
 template <> struct Store<LBM_STORE_BF16S> {
   using T = __nv_bfloat16;
   using R = float;
   __device__ static R ld(const T* p, int i) { return wf(i) + __bfloat162float(__ldg(p)); }
   __device__ static void st(T* p, R v, int i) { *p = __float2bfloat16_rn(v - wf(i)); }
+  __device__ static R to_r(T t, int i) { return wf(i) + __bfloat162float(t); }
+  __device__ static T from_r(R v, int i) { return __float2bfloat16_rn(v - wf(i)); }
 };
+
+// N contiguous elements, N * sizeof(T) bytes aligned to that size (up to 16)
+template <typename T, int N>
+__device__ __forceinline__ void ld_vec(const T* p, T out[N]) {
+  constexpr int B = N * (int)sizeof(T);
+  if constexpr (B % 16 == 0) {
+#pragma unroll
+    for (int j = 0; j < B / 16; ++j) {
+      const uint4 t = __ldg(reinterpret_cast<const uint4*>(p) + j);
+      memcpy(&out[j * (16 / sizeof(T))], &t, 16);
+    }
+  } else if constexpr (B == 8) {
+    const uint2 t = __ldg(reinterpret_cast<const uint2*>(p));
+    memcpy(out, &t, 8);
+  } else if constexpr (B == 4) {
+    const unsigned t = __ldg(reinterpret_cast<const unsigned*>(p));
+    memcpy(out, &t, 4);
+  } else {
+#pragma unroll
+    for (int j = 0; j < N; ++j) out[j] = p[j];
+  }
+}
+template <typename T, int N>
+__device__ __forceinline__ void st_vec(T* p, const T in[N]) {
+  constexpr int B = N * (int)sizeof(T);
+  if constexpr (B % 16 == 0) {
+#pragma unroll
+    for (int j = 0; j < B / 16; ++j) {
+      uint4 t;
+      memcpy(&t, &in[j * (16 / sizeof(T))], 16);
+      reinterpret_cast<uint4*>(p)[j] = t;
+    }
+  } else if constexpr (B == 8) {
+    uint2 t;
+    memcpy(&t, in, 8);
+    *reinterpret_cast<uint2*>(p) = t;
+  } else if constexpr (B == 4) {
+    unsigned t;
+    memcpy(&t, in, 4);
+    *reinterpret_cast<unsigned*>(p) = t;
+  } else {
+#pragma unroll
+    for (int j = 0; j < N; ++j) p[j] = in[j];
+  }
+}
 
 // ---------------------------------------------------------------------------
 // moments

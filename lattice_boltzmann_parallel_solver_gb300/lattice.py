@@ -35,7 +35,9 @@ class Lattice:
     """An nx x ny D2Q9 lattice with a fused boundary composition, resident on the device."""
 
     def __init__(self, nx: int, ny: int, omega: float, boundary=None, storage: str = "f64",
-                 exact: bool = False, device: str = "cuda"):
+                 exact: bool = False, device: str = "cuda", generic: bool = False, npt: int = 0):
+        """``generic`` forces the one-node-per-thread kernel; ``npt`` sets the
+        nodes per thread of the vectorised kernel (0 = the default for the storage)."""
         A.require_cuda()
         assert 0 < omega < 2
         assert storage in STORAGES, "storage must be one of %s" % sorted(STORAGES)
@@ -43,7 +45,8 @@ class Lattice:
         self.nx, self.ny, self.omega = int(nx), int(ny), float(omega)
         self.storage = storage
         self.store_id, self.pop_dtype, self.aux_dtype = STORAGES[storage]
-        self.flags = _lib.FLAG_EXACT if exact else 0
+        self.flags = (_lib.FLAG_EXACT if exact else 0) | (_lib.FLAG_GENERIC if generic else 0) | \
+            ((int(npt) & 15) << _lib.FLAG_NPT_SHIFT)
         self.pitch = (self.nx + 31) // 32 * 32
         self.device = torch.device(device)
         self.boundary = boundary

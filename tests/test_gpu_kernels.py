@@ -1,0 +1,65 @@
+"""The vectorised fused kernel (several nodes per thread, warp-shuffled x
+shifts) against the one-node-per-thread kernel, for every storage and
+nodes-per-thread choice, on geometries with walls, inlet/outlet, plate and
+the pressure rewrite, and on widths that leave partial warps and rows that
+are only two chunks wide."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import lbm_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pkg():
+    import lattice_boltzmann_parallel_solver_gb300 as P
+    P._lib.load()
+    return P
+
+
+def geometries(pkg, nx, ny):
+    U = pkg.boundary_utils
+    yield "periodic", None
+    yield "cavity", U.cavity_boundary_conditions(nx, ny, 0.1, 1.0)
+    yield "poiseuille", U.poiseuille_flow_boundary_conditions(nx, ny, (1 + 3e-3) / 3, (1 - 3e-3) / 3)
+    yield "vk", U.von_karman_boundary_conditions(nx, ny, 1.0, 0.1, max(2, ny // 5), walls=True)
+
+
+def start(nx, ny, seed):
+    rng = np.random.default_rng(seed)
+    rho = 1 + rng.normal(0, 0.01, (nx, ny))
+    u = rng.normal(0, 0.03, (nx, ny, 2))
+    return O.equilibrium(rho, u), rho, u
+
+
+TOL = {"f64": 1e-13, "f32": 1e-6, "f16": 1e-3, "bf16": 1e-2}
+
+
+@pytest.mark.parametrize("storage,npt", [("f64", 2), ("f64", 4), ("f32", 2), ("f32", 4), ("f16", 4),
+                                         ("f16", 8), ("bf16", 4), ("bf16", 8)])
+@pytest.mark.parametrize("nx,ny", [(16, 9), (48, 20), (520, 12), (1040, 7)])
+def test_vectorised_matches_generic(pkg, storage, npt, nx, ny):
+    if nx < 2 * npt or nx % npt:
+        pytest.skip("width not supported by this chunk size")
+    f, rho, u = start(nx, ny, nx * 7 + ny)
+    for name, bnd in geometries(pkg, nx, ny):
+        a = pkg.Lattice(nx, ny, 1.3, bnd, storage=storage, generic=True).set_state(f, rho, u).step(25)
+        b = pkg.Lattice(nx, ny, 1.3, bnd, storage=storage, npt=npt).set_state(f, rho, u).step(25)
+        fa, ra, ua = a.read()
+        fb, rb, ub = b.read()
+        err = float((fa - fb).abs().max() / fa.abs().max())
+        assert err <= TOL[storage], "%s %s: %.3e" % (name, storage, err)
+
+
+def test_vectorised_f64_against_oracle_with_pressure_and_outlet(pkg):
+    nx, ny = 64, 18
+    U = pkg.boundary_utils
+    f, rho, u = start(nx, ny, 3)
+    for obnd, bnd in ((O.poiseuille_boundary(nx, ny, 0.34, 0.33), U.poiseuille_flow_boundary_conditions(nx, ny, 0.34, 0.33)),
+                      (O.von_karman_boundary(nx, ny, 1.0, 0.1, 6), U.von_karman_boundary_conditions(nx, ny, 1.0, 0.1, 6))):
+        ref = O.run(f, rho, u, 1.4, 40, obnd)
+        lat = pkg.Lattice(nx, ny, 1.4, bnd, storage="f64", npt=2).set_state(f, rho, u).step(40)
+        got = lat.read()[0].cpu().numpy()
+        assert np.abs(got - ref[0]).max() / np.abs(ref[0]).max() <= 1e-12
