@@ -38,8 +38,185 @@ def parse():
     p.add_argument("--n", type=int, default=8192, help="cavity side")
     p.add_argument("--storage", default="f64", choices=sorted(BYTES_PER_NODE))
     p.add_argument("--exact", action="store_true", help="NumPy-order float64 arithmetic")
-    p.add_argument("--no-extras", action="store_true", help="skip variants, e2e and CPU baseline")
+    p.add_argument("--no-extras", action="store_true", help="skip variants, e2e, CPU baseline and the other configs")
+    p.add_argument("--workload", default="cavity", choices=["cavity", "shear", "vk", "batch", "serve"],
+                   help="cavity: the headline line; the others print one config's results and exit")
+    p.add_argument("--configs", default="shear,vk,batch,serve", help="other configs added to the headline line")
     return p.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# the other configurations (reported beside the headline)
+# ---------------------------------------------------------------------------
+def timed_ms(fn):
+    import torch
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1)
+
+
+def bench_shear(P):
+    """Shear-wave decay, float64, 64x64 periodic, omega 1.0, 2000 steps: amplitude
+    decay and the fitted viscosity by the reference's method
+    (experiments.py:195-210) against (1/omega - 1/2)/3; also the velocity shear wave."""
+    import torch
+    from scipy.optimize import curve_fit
+    from scipy.signal import argrelextrema
+    n, omega, steps = 64, 1.0, 2000
+    f, rho, u = P.scenarios.shear_wave(n, 0.01)
+    lat = P.Lattice(n, n, omega).set_state(f, rho, u)
+    amp = []
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        lat.step(1)
+        amp.append(lat.moments()[0] - 1.0)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    a = torch.stack(amp)
+    dens = torch.where(a.amin(dim=(1, 2)).abs() > a.amax(dim=(1, 2)).abs(), a.amin(dim=(1, 2)).abs(),
+                       a.amax(dim=(1, 2)).abs()).cpu().numpy()
+    idx = argrelextrema(dens, np.greater)[0]
+    k2 = (2 * np.pi / n) ** 2
+    nu_d = float(curve_fit(lambda t, v: 0.01 * np.exp(-v * k2 * t), idx, dens[idx], p0=[0.1])[0][0])
+    ux = P.initial_values.sinusoidal_velocity_x((n, n), 0.01)
+    lat = P.Lattice(n, n, omega).set_state(P.scenarios.equilibrium_np(*ux), *ux)
+    vel = []
+    for _ in range(400):
+        lat.step(5)
+        vel.append(float(lat.moments()[1][..., 0].abs().max()))
+    t = 5 * np.arange(1, 401)
+    nu_v = float(curve_fit(lambda t, v: 0.01 * np.exp(-v * k2 * t), t, np.array(vel), p0=[0.1])[0][0])
+    theory = (1 / omega - 0.5) / 3
+    return {"workload": "shear wave 64x64, omega 1.0, rho = 1 + 0.01 sin(2 pi x/64), 2000 steps, float64",
+            "amplitude_first_last": [float(dens[0]), float(dens[-1])], "nu_theory": theory,
+            "nu_fit_density_wave_reference_method": nu_d, "nu_fit_velocity_wave": nu_v,
+            "velocity_wave_rel_err": abs(nu_v - theory) / theory, "wall_s_with_per_step_readout": wall}
+
+
+def strouhal(trace, L=40, u=0.1, start=None):
+    """St from the FP64 FFT of a probe trace (visualizations_utils.py:157-160)."""
+    t = np.asarray(trace, dtype=np.float64)
+    if start is not None:
+        t = t[start:]
+    yf = np.fft.fft(t - t.mean())
+    freq = np.fft.fftfreq(len(t), 1)
+    return float(np.abs(freq[np.argmax(np.abs(yf))]) * L / u)
+
+
+def bench_vk(P, steps=100000):
+    """Von Karman precision study: 420x180, plate 40 at x=105 offset +1, inlet
+    (0.1, 0) with seeded U(-1e-3, 1e-3) u_y, the reference's outlet,
+    top/bottom bounce-back, Re 100; float64 against float32 / f16 / bf16
+    storage: velocity L2 error at fixed steps and the Strouhal number from
+    the FP64 FFT of u_y at (300, 90)."""
+    import torch
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch, Member
+    lx, ly = 420, 180
+    f, rho, u, omega, bnd = P.scenarios.von_karman(lx, ly, plate=40, re=100, seed=0)
+    checkpoints = [s for s in (10000, 50000, steps) if s <= steps]
+    out, ref_u = {}, {}
+    for storage in ("f64", "f32", "f16", "bf16"):
+        m = Member(lx, ly, omega, bnd, steps=steps, probe=(300, 90), f0=f, rho0=rho, u0=u)
+        b = Batch([m], storage=storage).start()
+        us, ms_total, done = {}, 0.0, 1
+        for c in checkpoints:
+            ms_total += timed_ms(lambda: b.run_graph(c - done, chunk=1000))
+            done = c
+            us[c] = b.read(0, want_f=False)[2]
+        uy = b.probe_trace(0)[:, 1].cpu().numpy()
+        res = {"mlups": lx * ly * (steps - 1) / (ms_total / 1e3) / 1e6,
+               "strouhal": strouhal(uy, start=len(uy) // 2)}
+        if storage == "f64":
+            ref_u = us
+            res["strouhal_reference"] = res["strouhal"]
+        else:
+            res["velocity_l2_rel_err"] = {str(c): float(torch.linalg.norm(us[c] - ref_u[c]) / torch.linalg.norm(ref_u[c]))
+                                          for c in checkpoints}
+            res["strouhal_rel_err"] = abs(res["strouhal"] - out["f64"]["strouhal"]) / out["f64"]["strouhal"]
+        out[storage] = res
+        del b, m
+    return {"workload": "von Karman 420x180, Re 100, %d steps, probe u_y at (300,90)" % steps, "storages": out}
+
+
+def bench_batch(P, steps=20000, n=256):
+    """Batched sweep: 256 von Karman lattices (nx ~ U{200..1200}, ny = nx U(0.3,0.5)
+    even, plate ny U(0.1,0.3), Re log-uniform [40, 250], inlet 0.1), f16 storage,
+    autotuned tiles, graph-captured; against the same lattices solved one by one
+    in plain float64 (timed on a sample, extrapolated)."""
+    import torch
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch, Member, autotune
+    params = P.scenarios.batch_sweep_params(n)
+    members = []
+    for j, q in enumerate(params):
+        f, rho, u, om, bnd = P.scenarios.von_karman_device(q["nx"], q["ny"], q["plate"], q["re"], seed=j)
+        members.append(Member(q["nx"], q["ny"], om, bnd, steps=steps, f0=f, rho0=rho, u0=u))
+    b = Batch(members, storage="f16")
+    tune = autotune(b, steps=4, warmup=2)
+    b.start()
+    ms = timed_ms(lambda: b.run_graph(chunk=200))
+    nodes = sum(m.nodes for m in members)
+    agg = nodes * (steps - 1) / (ms / 1e3) / 1e6
+    del b
+    for m in members:
+        m.pop, m.aux = [], []
+    torch.cuda.empty_cache()
+    # plain float64 one at a time, each on its own resident lattice, on a sample
+    rng = np.random.default_rng(1)
+    sample = rng.choice(n, size=12, replace=False)
+    t64, nodes64 = 0.0, 0
+    for j in sample:
+        m = members[j]
+        lat = P.Lattice(m.nx, m.ny, m.omega, m.boundary, storage="f64").set_state(m.f0, m.rho0, m.u0)
+        lat.step(3)
+        k = 300
+        t64 += timed_ms(lambda: lat.step_graph(k, chunk=100)) / 1e3
+        nodes64 += m.nodes * k
+        del lat
+    rate64 = nodes64 / t64
+    seq_s = nodes * steps / rate64
+    best = min(tune, key=lambda r: r["ms_per_step"])
+    return {"workload": "%d von Karman lattices, %d steps each, %.1f M nodes, f16 storage" % (n, steps, nodes / 1e6),
+            "aggregate_mlups": agg, "batch_wall_s": ms / 1e3, "autotuned": best,
+            "candidates": len(tune), "f64_sequential_mlups": rate64 / 1e6,
+            "f64_sequential_wall_s_extrapolated": seq_s, "speedup_vs_sequential_f64": seq_s / (ms / 1e3),
+            "omega_range": [min(q["omega"] for q in params), max(q["omega"] for q in params)],
+            "stability_risk_instances": sum(q["risky"] for q in params)}
+
+
+def bench_serve(P, n16=200, n64=40):
+    """Serving: seeded Poisson arrivals at 50/s of Couette / Poiseuille / von
+    Karman requests with 1k-50k steps, continuous batching under an HBM budget;
+    f16 storage against plain float64; error of f16 results against their solo
+    float64 solve on a sample."""
+    import torch
+    from lattice_boltzmann_parallel_solver_gb300.serving import ServingEngine, request_mix, summarize
+    out = {}
+    for storage, n in (("f16", n16), ("f64", n64)):
+        reqs = request_mix(n, rate=50.0, seed=7)
+        eng = ServingEngine(storage=storage, hbm_budget=64 << 30, tick_steps=500)
+        done = eng.serve(reqs, realtime=True)
+        s = summarize(done)
+        s["max_live"] = eng.stats["max_live"]
+        out[storage] = s
+        if storage == "f16":
+            errs, budget = {}, 0.0
+            for r in sorted(done, key=lambda r: r.nodes * r.steps):
+                if budget > 20.0 or len(errs) >= 9:
+                    break
+                lat = P.Lattice(r.nx, r.ny, r.omega, r.boundary, storage="f64").set_state(r.f0, r.rho0, r.u0)
+                t = timed_ms(lambda: lat.step(r.steps)) / 1e3
+                budget += t
+                u64 = lat.moments()[1]
+                errs.setdefault(r.kind, []).append(float(torch.linalg.norm(r.u - u64) / torch.linalg.norm(u64)))
+            out["f16_velocity_l2_rel_err_vs_solo_f64"] = {k: max(v) for k, v in errs.items()}
+        del done, reqs
+        torch.cuda.empty_cache()
+    return {"workload": "Poisson 50 req/s mix of Couette / Poiseuille / von Karman, 1k-50k steps, "
+                        "HBM budget 64 GB", "results": out}
 
 
 def peaks():
@@ -191,6 +368,10 @@ def main():
     from lattice_boltzmann_parallel_solver_gb300.lattice_boltzmann_method import lattice_boltzmann_step
 
     torch.cuda.set_device(local)
+    if args.workload != "cavity":
+        fn = {"shear": bench_shear, "vk": bench_vk, "batch": bench_batch, "serve": bench_serve}[args.workload]
+        print(json.dumps(fn(P)), flush=True)
+        return
     if world > 1:
         dist.init_process_group("nccl")
 
@@ -265,15 +446,13 @@ def main():
         f_h.copy_(w.cpu().expand(n, n, 9))
         rho_h = torch.ones((n, n), dtype=torch.float64).pin_memory()
         u_h = torch.zeros((n, n, 2), dtype=torch.float64).pin_memory()
-        e2e_steps = 3
+        e2e_steps = 5
         state = lattice_boltzmann_step(f_h, rho_h, u_h, 1.7, bnd)
         barrier()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
-            state = lattice_boltzmann_step(f_h, rho_h, u_h, 1.7, bnd)
-            f_h.copy_(state[0])
-            rho_h.copy_(state[1])
-            u_h.copy_(state[2])
+            # inputs come from pinned host memory, results land in pinned host memory
+            state = lattice_boltzmann_step(*state, 1.7, bnd)
         barrier()
         e2e_secs = slowest(time.perf_counter() - t0)
         bytes_io = (f_h.numel() + rho_h.numel() + u_h.numel()) * 8
@@ -284,6 +463,16 @@ def main():
         del f_h, rho_h, u_h, state
         if rank == 0 and world == 1:
             extras["cpu_baseline"] = cpu_baseline_single()
+        if rank == 0:
+            configs = {}
+            for name in [c for c in args.configs.split(",") if c]:
+                fn = {"shear": bench_shear, "vk": bench_vk, "batch": bench_batch, "serve": bench_serve}[name]
+                try:
+                    configs[name] = fn(P)
+                except Exception as exc:  # a side configuration must not lose the headline line
+                    configs[name] = {"error": "%s: %s" % (type(exc).__name__, exc)}
+                torch.cuda.empty_cache()
+            extras["configs"] = configs
 
     if rank != 0:
         return

@@ -161,6 +161,41 @@ int lbm_lattice_run(const lbm_geometry* g, int32_t storage, void* pop_a, void* p
 int lbm_lattice_read(const lbm_geometry* g, int32_t storage, const void* pop, int64_t pitch,
                      const void* aux, double* f_out, double* rho_out, double* u_out, void* stream);
 
+/* ---- batched lattices ----------------------------------------------------------- */
+/* Many lattices of different sizes, one storage type, advanced together: one
+ * launch per time step covers every live lattice (a flat list of row-segment
+ * tiles walked by a persistent grid).  Lattice j is live for global steps
+ * [s0, s_end); at global step g it reads pop_a when (g - s0) is even.  The
+ * global step is *gbase (device int) plus the launch's index, and
+ * lbm_batch_run ends with a kernel adding nsteps to *gbase, so a captured
+ * CUDA graph of one lbm_batch_run call can be replayed.  The probe, when
+ * probe_buf is set, appends (ux, uy) of node (probe_x, probe_y) each step at
+ * probe_buf[2 * (*probe_count)++] while the count is below probe_cap.
+ * No reference counterpart as a whole: it runs many drivers' loops
+ * (src/experiments.py:650-720) at once. */
+typedef struct lbm_batch_lattice {
+  const lbm_geometry* g;
+  void* pop_a;
+  void* pop_b;
+  void* aux_a;
+  void* aux_b;
+  int64_t pitch;
+  double omega;
+  int32_t s0, s_end;
+  int32_t probe_x, probe_y, probe_cap;
+  double* probe_buf;
+  int32_t* probe_count;
+} lbm_batch_lattice;
+
+size_t lbm_batch_table_bytes(int32_t n);
+/* Writes the device work table (table_bytes >= lbm_batch_table_bytes(n)) for
+ * tiles of `threads` threads x `npt` nodes; synchronises `stream`. */
+int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_t threads, void* table,
+                    size_t table_bytes, int32_t* total_tiles, void* stream);
+/* nsteps batched steps with `blocks` persistent blocks (0 = fill the GPU). */
+int lbm_batch_run(const void* table, int32_t n, int32_t total_tiles, int32_t storage, int32_t npt,
+                  int32_t threads, int32_t* gbase, int32_t nsteps, int32_t blocks, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -43,11 +43,14 @@ def to_device(a, dtype=torch.float64) -> torch.Tensor:
 
 
 def to_kind(t: torch.Tensor, kind: int):
+    """Device result back in the caller's kind; host results land in pinned
+    memory (the caching host allocator reuses it across calls)."""
     if kind == TORCH_CUDA:
         return t
-    if kind == TORCH_CPU:
-        return t.cpu()
-    return t.cpu().numpy()
+    out = torch.empty(t.shape, dtype=t.dtype, pin_memory=True)
+    out.copy_(t, non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    return out if kind == TORCH_CPU else out.numpy()
 
 
 def write_back(dst, src: torch.Tensor):

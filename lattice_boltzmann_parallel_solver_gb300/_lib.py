@@ -48,6 +48,13 @@ class Geometry(C.Structure):
 
 GP = C.POINTER(Geometry)
 
+
+class BatchLattice(C.Structure):
+    """lbm_batch_lattice in include/lbm_gb300.h"""
+    _fields_ = [("g", vp), ("pop_a", vp), ("pop_b", vp), ("aux_a", vp), ("aux_b", vp), ("pitch", i64),
+                ("omega", f64), ("s0", i32), ("s_end", i32), ("probe_x", i32), ("probe_y", i32),
+                ("probe_cap", i32), ("probe_buf", vp), ("probe_count", vp)]
+
 # name: (restype, argtypes)
 SIGNATURES = {
     "lbm_version": (C.c_int, []),
@@ -68,6 +75,9 @@ SIGNATURES = {
     "lbm_lattice_init": (C.c_int, [GP, i32, vp, vp, vp, f64, vp, i64, vp, i32, vp]),
     "lbm_lattice_run": (C.c_int, [GP, i32, vp, vp, i64, vp, vp, f64, i32, vp, vp, i32, vp]),
     "lbm_lattice_read": (C.c_int, [GP, i32, vp, i64, vp, vp, vp, vp, vp]),
+    "lbm_batch_table_bytes": (C.c_size_t, [i32]),
+    "lbm_batch_build": (C.c_int, [C.POINTER(BatchLattice), i32, i32, i32, vp, C.c_size_t, C.POINTER(i32), vp]),
+    "lbm_batch_run": (C.c_int, [vp, i32, i32, i32, i32, i32, vp, i32, i32, vp]),
 }
 
 _lib = None

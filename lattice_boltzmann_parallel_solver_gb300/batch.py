@@ -1,0 +1,261 @@
+"""Many lattices of different sizes advanced together: one kernel launch per
+time step covers every live lattice (a flat list of row-segment tiles walked
+by a persistent grid), optionally replayed from a captured CUDA graph.
+
+This runs what the reference does one driver loop at a time - for example
+the Reynolds / blockage / width sweeps of ``x_strouhal``
+(src/experiments.py:650-720, src/main.py:150-207) - as one device job.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+from dataclasses import dataclass, field
+
+import torch
+
+from . import _arrays as A
+from . import _lib
+from .geometry import empty_geometry
+from .lattice import STORAGES
+
+
+BatchLatticeC = _lib.BatchLattice
+
+
+@dataclass
+class Member:
+    """One lattice of a batch: its geometry, state buffers and step window."""
+    nx: int
+    ny: int
+    omega: float
+    boundary: object = None
+    steps: int = 1
+    probe: tuple = None          # (x, y) node whose velocity is recorded every step
+    f0: object = None            # reference-layout initial populations
+    rho0: object = None
+    u0: object = None
+    # filled in by the batch
+    geo: object = None
+    pitch: int = 0
+    pop: list = field(default_factory=list)
+    aux: list = field(default_factory=list)
+    probe_buf: torch.Tensor = None
+    probe_count: torch.Tensor = None
+    s0: int = 0
+
+    @property
+    def nodes(self) -> int:
+        return self.nx * self.ny
+
+
+class Batch:
+    """A set of lattices sharing one storage type, advanced in lock step.
+    Members can join (``add``) and leave (``remove``) between runs."""
+
+    def __init__(self, members=(), storage: str = "f16", npt: int = 0, threads: int = 128, blocks: int = 0,
+                 device: str = "cuda"):
+        A.require_cuda()
+        self.storage = storage
+        self.store_id, self.pop_dtype, self.aux_dtype = STORAGES[storage]
+        self.device = torch.device(device)
+        self.npt = npt or (2 if storage == "f64" else 4)
+        self.threads = threads
+        self.blocks = blocks
+        self.gbase = torch.zeros(1, dtype=torch.int32, device=self.device)
+        self.g = 0                    # host mirror of the global step
+        self.members = []
+        for m in members:
+            self._alloc(m)
+            self.members.append(m)
+        self.table = None
+        self.tiles = 0
+        self._dirty = True
+        self._graphs = {}
+
+    def _alloc(self, m: Member):
+        m.geo = m.boundary.geometry(m.nx, m.ny) if m.boundary is not None else empty_geometry(m.nx, m.ny)
+        if not m.geo.fusable:
+            raise NotImplementedError("the outlet must sit on column nx-1")
+        m.pitch = (m.nx + 31) // 32 * 32
+        n = 9 * m.ny * m.pitch
+        m.pop = [torch.empty(n, dtype=self.pop_dtype, device=self.device) for _ in range(2)]
+        m.aux = [torch.zeros(3 * m.ny, dtype=self.aux_dtype, device=self.device) for _ in range(2)]
+        if m.probe is not None:
+            m.probe_buf = torch.zeros(2 * max(m.steps, 1), dtype=torch.float64, device=self.device)
+            m.probe_count = torch.zeros(1, dtype=torch.int32, device=self.device)
+
+    def _init_member(self, m: Member):
+        """The member's first step (collision of its initial state); its remaining
+        steps are global steps [g, g + steps - 1)."""
+        f = A.to_device(m.f0)
+        rho = A.to_device(m.rho0) if m.rho0 is not None else None
+        u = A.to_device(m.u0) if m.u0 is not None else None
+        _lib.call("lbm_lattice_init", m.geo.ref, self.store_id, f.data_ptr(), A.ptr(rho), A.ptr(u), m.omega,
+                  m.pop[0].data_ptr(), m.pitch, m.aux[0].data_ptr(), 0, A.stream())
+        m.s0 = self.g
+        if m.probe_count is not None:
+            m.probe_count.zero_()
+
+    def add(self, m: Member):
+        """Admit a lattice now: allocate, take its first step, join the next launch."""
+        self._alloc(m)
+        self._init_member(m)
+        self.members.append(m)
+        self._dirty = True
+        return m
+
+    def remove(self, m: Member):
+        """Drop a lattice and release its device memory."""
+        self.members = [x for x in self.members if x is not m]
+        m.pop, m.aux = [], []
+        self._dirty = True
+
+    def done(self, m: Member) -> bool:
+        return self.g >= m.s0 + m.steps - 1
+
+    @property
+    def nodes(self) -> int:
+        return sum(m.nodes for m in self.members)
+
+    @property
+    def state_bytes(self) -> int:
+        return sum(t.numel() * t.element_size() for m in self.members for t in m.pop + m.aux)
+
+    # -- work table ----------------------------------------------------------------
+    def _build(self, with_probes=True):
+        n = len(self.members)
+        arr = (BatchLatticeC * n)()
+        self._keep = []
+        for j, m in enumerate(self.members):
+            c = arr[j]
+            c.g = ctypes.addressof(m.geo.struct)
+            c.pop_a, c.pop_b = m.pop[0].data_ptr(), m.pop[1].data_ptr()
+            c.aux_a, c.aux_b = m.aux[0].data_ptr(), m.aux[1].data_ptr()
+            c.pitch, c.omega = m.pitch, m.omega
+            c.s0, c.s_end = m.s0, m.s0 + max(m.steps - 1, 0)
+            if with_probes and m.probe is not None:
+                c.probe_x, c.probe_y = int(m.probe[0]), int(m.probe[1])
+                c.probe_cap = m.probe_buf.numel() // 2
+                c.probe_buf, c.probe_count = m.probe_buf.data_ptr(), m.probe_count.data_ptr()
+            else:
+                c.probe_x = c.probe_y = -1
+        size = int(_lib.load().lbm_batch_table_bytes(n))
+        self.table = torch.empty(size, dtype=torch.uint8, device=self.device)
+        tiles = ctypes.c_int32(0)
+        _lib.call("lbm_batch_build", arr, n, self.npt, self.threads, self.table.data_ptr(), size,
+                  ctypes.byref(tiles), A.stream())
+        self.tiles = tiles.value
+        self._graphs.clear()
+        self._dirty = False
+
+    # -- state ---------------------------------------------------------------------
+    def start(self):
+        """Take every member's first step and arm the batch at the current global step."""
+        for m in self.members:
+            self._init_member(m)
+        self._build()
+        return self
+
+    @property
+    def remaining(self) -> int:
+        return max((m.s0 + m.steps - 1 for m in self.members), default=self.g) - self.g
+
+    def run(self, nsteps: int = None):
+        """Advance nsteps global steps (default: until every member is done)."""
+        n = self.remaining if nsteps is None else int(nsteps)
+        if self._dirty and self.members:
+            self._build()
+        if n > 0 and self.members:
+            _lib.call("lbm_batch_run", self.table.data_ptr(), len(self.members), self.tiles, self.store_id,
+                      self.npt, self.threads, self.gbase.data_ptr(), n, self.blocks, A.stream())
+            self.g += n
+        return self
+
+    def run_graph(self, nsteps: int = None, chunk: int = 100):
+        """Like run(), replaying a captured graph of ``chunk`` steps."""
+        n = self.remaining if nsteps is None else int(nsteps)
+        if self._dirty and self.members:
+            self._build()
+        full, rest = divmod(max(n, 0), chunk)
+        if full:
+            g = self._graphs.get(chunk)
+            if g is None:
+                # a zero-step call outside capture settles the default grid size
+                _lib.call("lbm_batch_run", self.table.data_ptr(), len(self.members), self.tiles, self.store_id,
+                          self.npt, self.threads, self.gbase.data_ptr(), 0, self.blocks, A.stream())
+                g = torch.cuda.CUDAGraph()
+                side = torch.cuda.Stream()
+                side.wait_stream(torch.cuda.current_stream())
+                with torch.cuda.stream(side):
+                    with torch.cuda.graph(g, stream=side):
+                        _lib.call("lbm_batch_run", self.table.data_ptr(), len(self.members), self.tiles,
+                                  self.store_id, self.npt, self.threads, self.gbase.data_ptr(), chunk, self.blocks,
+                                  side.cuda_stream)
+                torch.cuda.current_stream().wait_stream(side)
+                self._graphs[chunk] = g
+            for _ in range(full):
+                g.replay()
+            self.g += full * chunk
+        if rest:
+            self.run(rest)
+        return self
+
+    def current(self, m: Member) -> int:
+        """Index of the buffer holding member m's state at the current global step."""
+        done = min(max(self.g - m.s0, 0), max(m.steps - 1, 0))
+        return done % 2
+
+    def read(self, j, want_f: bool = True):
+        """(f, rho, u) of member j (an index or the Member) in the reference layout (float64, device)."""
+        m = self.members[j] if isinstance(j, int) else j
+        k = self.current(m)
+        f = torch.empty((m.nx, m.ny, 9), dtype=torch.float64, device=self.device) if want_f else None
+        rho = torch.empty((m.nx, m.ny), dtype=torch.float64, device=self.device)
+        u = torch.empty((m.nx, m.ny, 2), dtype=torch.float64, device=self.device)
+        _lib.call("lbm_lattice_read", m.geo.ref, self.store_id, m.pop[k].data_ptr(), m.pitch, m.aux[k].data_ptr(),
+                  A.ptr(f), rho.data_ptr(), u.data_ptr(), A.stream())
+        return f, rho, u
+
+    def probe_trace(self, j: int) -> torch.Tensor:
+        """Velocity (ux, uy) recorded at member j's probe, one row per batched step."""
+        m = self.members[j]
+        n = min(int(m.probe_count.item()), m.probe_buf.numel() // 2)
+        return m.probe_buf[: 2 * n].view(n, 2)
+
+
+def autotune(batch: Batch, candidates=None, steps: int = 6, warmup: int = 2):
+    """Pick nodes per thread, threads per block and persistent grid size for a
+    batch by timing each candidate on the batch itself.  Call it before
+    ``start()``: the timed steps run on the members' uninitialised buffers
+    (probes off) and the global step counter is reset afterwards."""
+    sms = torch.cuda.get_device_properties(batch.device).multi_processor_count
+    if candidates is None:
+        npts = (2,) if batch.storage == "f64" else (2, 4, 8) if batch.storage in ("f16", "bf16") else (2, 4)
+        candidates = [(p, t, b) for p in npts for t in (64, 128, 256) for b in (0, 2 * sms, 8 * sms)]
+    best, results = None, []
+    for npt, threads, blocks in candidates:
+        batch.npt, batch.threads, batch.blocks = npt, threads, blocks
+        try:
+            batch._build(with_probes=False)
+        except (AssertionError, NotImplementedError):
+            continue
+        batch.run(warmup)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        batch.run(steps)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        results.append({"npt": npt, "threads": threads, "blocks": blocks, "ms_per_step": ms,
+                        "glups": batch.nodes / (ms * 1e-3) / 1e9})
+        if best is None or ms < best[0]:
+            best = (ms, npt, threads, blocks)
+        del t0
+    batch.g = 0
+    batch.gbase.zero_()
+    _, batch.npt, batch.threads, batch.blocks = best
+    batch.tuning = results
+    return results

@@ -104,12 +104,14 @@ def plate_rows(ly, plate_size):
             ly // 2 + plate_size // 2 - 1, ly // 2 - plate_size // 2)
 
 
-def _vk_closures(lx, ly, density_in, velocity_in, plate_size, off=0, plate_x=None, walls=False, feq_in=None):
+def _vk_closures(lx, ly, density_in, velocity_in, plate_size, off=0, plate_x=None, walls=False, feq_in=None,
+                 plate_offset=0):
     """Inlet, outlet, plate left face + corners, plate right face + corners, on
     a domain whose interior starts at index ``off`` (1 for ghost-padded arrays).
-    ``feq_in`` (the 9 inlet populations) is computed on the device when not given."""
+    ``feq_in`` (the 9 inlet populations) is computed on the device when not given;
+    ``plate_offset`` shifts the plate rows."""
     px = (lx // 4 if plate_x is None else plate_x) + off
-    y_min, y_max, y_up, y_lo = plate_rows(ly, plate_size)
+    y_min, y_max, y_up, y_lo = (r + plate_offset for r in plate_rows(ly, plate_size))
     if feq_in is None:
         feq_in = inlet((1, ly), density_in, velocity_in).values
 
@@ -156,11 +158,13 @@ def parallel_von_karman_boundary_conditions(coord2d, n_local_x, n_local_y, lx, l
     return Boundary(_vk_closures(lx, ly, density_in, velocity_in, plate_size, off=1), padded=True)
 
 
-def von_karman_boundary_conditions(lx, ly, density_in, velocity_in, plate_size, plate_x=None, walls=False):
+def von_karman_boundary_conditions(lx, ly, density_in, velocity_in, plate_size, plate_x=None, walls=False,
+                                   plate_offset=0):
     """The same composition on an unpadded periodic lx x ly lattice (fusable).
-    ``walls=True`` adds rigid bottom/top rows after the plate."""
+    ``walls=True`` adds rigid bottom/top rows after the plate; ``plate_offset``
+    moves the plate by that many rows."""
     return Boundary(_vk_closures(lx, ly, density_in, velocity_in, plate_size, off=0, plate_x=plate_x,
-                                 walls=walls))
+                                 walls=walls, plate_offset=plate_offset))
 
 
 def cavity_boundary_conditions(nx, ny, u_lid=0.1, avg_density=1.0):

@@ -1,0 +1,157 @@
+// lbm_batch.cu -- many lattices of different sizes advanced by one launch per
+// time step (the batched sweep and the serving loop run on it).
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "lbm_fused.cuh"
+
+namespace lbm {
+
+template <int STORE, int NPT, int THREADS>
+__global__ void __launch_bounds__(THREADS) batch_kernel(const BatchEntry* __restrict__ tab,
+                                                        const int* __restrict__ tile_start, int n_inst,
+                                                        int total_tiles, const int* __restrict__ gbase, int k) {
+  const int g = *gbase + k;
+  for (int tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
+    int lo = 0, hi = n_inst - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(tile_start + mid) <= tile) lo = mid;
+      else hi = mid - 1;
+    }
+    const BatchEntry& e = tab[lo];
+    if (g < e.s0 || g >= e.s_end) continue;
+    const int local = tile - __ldg(tile_start + lo);
+    const int y = local / e.xblocks, xb = local - y * e.xblocks;
+    const bool odd = (g - e.s0) & 1;
+    fused_v2_body<STORE, NPT, true, true>(e.P, odd ? e.pop_b : e.pop_a, odd ? e.pop_a : e.pop_b,
+                                          odd ? e.aux_b : e.aux_a, odd ? e.aux_a : e.aux_b,
+                                          (xb * THREADS + threadIdx.x) * NPT, y);
+  }
+}
+
+__global__ void batch_advance_kernel(int* gbase, int k) { *gbase += k; }
+
+}  // namespace lbm
+
+using namespace lbm;
+
+extern "C" {
+
+size_t lbm_batch_table_bytes(int32_t n) {
+  return (size_t)n * sizeof(BatchEntry) + (size_t)n * sizeof(int) + 256;
+}
+
+int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_t threads, void* table,
+                    size_t table_bytes, int32_t* total_tiles, void* stream) {
+  if (lat == nullptr || n < 1 || table == nullptr || total_tiles == nullptr)
+    return set_error(LBM_ERR_ARG, "bad batch arguments");
+  if (table_bytes < lbm_batch_table_bytes(n)) return set_error(LBM_ERR_ARG, "batch table buffer too small");
+  if (!(npt == 2 || npt == 4 || npt == 8) || !(threads == 64 || threads == 128 || threads == 256))
+    return set_error(LBM_ERR_ARG, "npt must be 2, 4 or 8 and threads 64, 128 or 256");
+  if ((uintptr_t)table % 16 != 0) return set_error(LBM_ERR_ARG, "batch table must be 16-byte aligned");
+  std::vector<BatchEntry> ent((size_t)n);
+  std::vector<int> start((size_t)n);
+  int64_t tiles = 0;
+  for (int j = 0; j < n; ++j) {
+    const lbm_batch_lattice& L = lat[j];
+    BatchEntry& e = ent[(size_t)j];
+    std::memset(&e, 0, sizeof(e));
+    if (!to_geok(L.g, e.P.g)) return last_status();
+    if (int st = check_omega(L.omega)) return st;
+    if (int st = check_pitch(L.g->nx, L.pitch)) return st;
+    if (L.pop_a == nullptr || L.pop_b == nullptr) return set_error(LBM_ERR_ARG, "batch lattice without buffers");
+    if (L.g->outlet && (L.aux_a == nullptr || L.aux_b == nullptr))
+      return set_error(LBM_ERR_ARG, "batch lattice with an outlet needs aux buffers");
+    e.P.pitch = L.pitch;
+    e.P.plane = L.pitch * L.g->ny;
+    e.P.omega = L.omega;
+    e.P.pop_in = L.pop_a;
+    e.P.pop_out = L.pop_b;
+    e.P.probe_x = L.probe_x;
+    e.P.probe_y = L.probe_y;
+    e.P.probe_cap = L.probe_cap;
+    e.P.probe_buf = L.probe_buf;
+    e.P.probe_count = L.probe_count;
+    if (L.probe_buf != nullptr && L.probe_count == nullptr)
+      return set_error(LBM_ERR_ARG, "a probe needs its counter");
+    if (!v2_fits(e.P, npt)) return set_error(LBM_ERR_UNSUPPORTED, "a batch lattice is too narrow or too large for npt");
+    e.pop_a = L.pop_a;
+    e.pop_b = L.pop_b;
+    e.aux_a = L.aux_a;
+    e.aux_b = L.aux_b;
+    e.s0 = L.s0;
+    e.s_end = L.s_end;
+    const int chunks = (L.g->nx + npt - 1) / npt;
+    e.xblocks = (chunks + threads - 1) / threads;
+    start[(size_t)j] = (int)tiles;
+    tiles += (int64_t)e.xblocks * L.g->ny;
+  }
+  if (tiles >= ((int64_t)1 << 31)) return set_error(LBM_ERR_ARG, "too many tiles");
+  char* dst = static_cast<char*>(table);
+  cudaError_t err = cudaMemcpyAsync(dst, ent.data(), ent.size() * sizeof(BatchEntry), cudaMemcpyHostToDevice,
+                                    (cudaStream_t)stream);
+  if (err == cudaSuccess)
+    err = cudaMemcpyAsync(dst + ent.size() * sizeof(BatchEntry), start.data(), start.size() * sizeof(int),
+                          cudaMemcpyHostToDevice, (cudaStream_t)stream);
+  if (err == cudaSuccess) err = cudaStreamSynchronize((cudaStream_t)stream);
+  if (err != cudaSuccess) return set_error(LBM_ERR_CUDA, cudaGetErrorString(err));
+  *total_tiles = (int32_t)tiles;
+  return LBM_OK;
+}
+
+}  // extern "C"
+
+template <int STORE, int NPT, int THREADS>
+static int launch_batch(const void* table, int n, int tiles, int* gbase, int nsteps, int blocks, cudaStream_t s) {
+  const BatchEntry* tab = static_cast<const BatchEntry*>(table);
+  const int* start = reinterpret_cast<const int*>(static_cast<const char*>(table) + (size_t)n * sizeof(BatchEntry));
+  if (blocks <= 0) {
+    // resident blocks of this kernel on the whole GPU, queried on the first
+    // call (make that call outside stream capture) and reused afterwards
+    static int fill = 0;
+    if (fill == 0) {
+      int per_sm = 0, sms = 0, dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<STORE, NPT, THREADS>, THREADS, 0);
+      fill = std::max(1, sms * std::max(1, per_sm));
+    }
+    blocks = fill;
+  }
+  blocks = std::min(blocks, std::max(1, tiles));
+  for (int k = 0; k < nsteps; ++k) {
+    batch_kernel<STORE, NPT, THREADS><<<blocks, THREADS, 0, s>>>(tab, start, n, tiles, gbase, k);
+    count_launch();
+    if (int e = check_launch("batch_kernel")) return e;
+  }
+  batch_advance_kernel<<<1, 1, 0, s>>>(gbase, nsteps);
+  count_launch();
+  return check_launch("batch_advance_kernel");
+}
+
+extern "C" int lbm_batch_run(const void* table, int32_t n, int32_t total_tiles, int32_t storage, int32_t npt,
+                             int32_t threads, int32_t* gbase, int32_t nsteps, int32_t blocks, void* stream) {
+  if (table == nullptr || gbase == nullptr || n < 1 || total_tiles < 0 || nsteps < 0)
+    return set_error(LBM_ERR_ARG, "bad batch run arguments");
+  cudaStream_t s = (cudaStream_t)stream;
+#define LBM_BATCH_CASE(ST, NP, TH) \
+  if (storage == ST && npt == NP && threads == TH) return launch_batch<ST, NP, TH>(table, n, total_tiles, gbase, nsteps, blocks, s);
+#define LBM_BATCH_NPT(ST, NP) LBM_BATCH_CASE(ST, NP, 64) LBM_BATCH_CASE(ST, NP, 128) LBM_BATCH_CASE(ST, NP, 256)
+  LBM_BATCH_NPT(LBM_STORE_F64, 2)
+  LBM_BATCH_NPT(LBM_STORE_F64, 4)
+  LBM_BATCH_NPT(LBM_STORE_F32, 2)
+  LBM_BATCH_NPT(LBM_STORE_F32, 4)
+  LBM_BATCH_NPT(LBM_STORE_F16S, 2)
+  LBM_BATCH_NPT(LBM_STORE_F16S, 4)
+  LBM_BATCH_NPT(LBM_STORE_F16S, 8)
+  LBM_BATCH_NPT(LBM_STORE_BF16S, 2)
+  LBM_BATCH_NPT(LBM_STORE_BF16S, 4)
+  LBM_BATCH_NPT(LBM_STORE_BF16S, 8)
+#undef LBM_BATCH_NPT
+#undef LBM_BATCH_CASE
+  return set_error(LBM_ERR_UNSUPPORTED, "no batched kernel for this storage / npt / threads");
+}
+
+

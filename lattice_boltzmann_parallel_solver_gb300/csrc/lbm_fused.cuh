@@ -1,0 +1,310 @@
+// lbm_fused.cuh -- parameters and the vectorised fused-step body shared by the
+// single-lattice kernels (lbm_lattice.cu) and the batched kernels (lbm_batch.cu).
+#pragma once
+#include <algorithm>
+#include <cstring>
+
+#include "lbm_core.cuh"
+#include "lbm_host.h"
+
+namespace lbm {
+
+enum { MODE_INIT = 0, MODE_FUSED = 1, MODE_READ = 2 };
+
+struct GeoK {
+  int nx, ny, words;
+  const uint32_t* bcmask;
+  const uint32_t* desc;
+  int pressure;
+  uint32_t pin, pout;
+  double rho_in, rho_out;
+  int outlet;
+  double kconst[LBM_MAX_SETS][9];
+  double cconst[LBM_MAX_SETS][9];
+};
+
+struct View {
+  const double* p;
+  int64_t sx, sy, sc;
+};
+struct OutView {
+  double* p;
+  int64_t sx, sy, sc;
+};
+
+struct KParams {
+  GeoK g;
+  const void* pop_in;
+  void* pop_out;
+  int64_t pitch, plane;
+  const void* aux_in;
+  void* aux_out;
+  View f_in, rho_in, u_in;
+  OutView f_out, rho_out, u_out;
+  double omega;
+  // optional probe: the fused step at node (probe_x, probe_y) appends its
+  // pre-collision velocity to probe_buf[2 * t], t = (*probe_count)++
+  int probe_x, probe_y, probe_cap;
+  double* probe_buf;
+  int* probe_count;
+};
+
+template <typename R>
+__device__ __forceinline__ void write_probe(const KParams& P, int x, int y, R ux, R uy) {
+  if (P.probe_buf != nullptr && x == P.probe_x && y == P.probe_y) {
+    const int t = *P.probe_count;
+    if (t < P.probe_cap) {
+      P.probe_buf[2 * t] = (double)ux;
+      P.probe_buf[2 * t + 1] = (double)uy;
+    }
+    *P.probe_count = t + 1;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Vectorised fused step.  Each thread owns NPT consecutive nodes of one row
+// (one aligned vector per population plane).  The six planes with cx = +-1
+// need the chunk shifted by one node: the missing element comes from the
+// neighbouring lane by a warp shuffle, or by a direct load at the first and
+// last lane of a warp and at the row ends (periodic wrap).  A row whose width
+// is not a multiple of NPT ends in a partial chunk: its vector loads run into
+// the row padding (pitch >= nx rounded up to 32), the node at nx-1 takes its
+// cx = -1 populations from x = 0, and it stores node by node.  Offsets are
+// 32-bit element indices (9 * plane < 2^31).  Boundary descriptors and the
+// pressure rewrite are compiled in only where a geometry may have them.
+// ---------------------------------------------------------------------------
+template <int STORE, int NPT, bool HAS_BC, bool HAS_PRESSURE>
+__device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_in_v, void* pop_out_v,
+                                              const void* aux_in_v, void* aux_out_v, int x0, int y) {
+  using St = Store<STORE>;
+  using T = typename St::T;
+  using R = typename St::R;
+  const int lane = threadIdx.x & 31;
+  const int nx = P.g.nx, ny = P.g.ny;
+  const int xlast = ((nx - 1) / NPT) * NPT;  // first node of the last chunk of a row
+  const bool active = x0 < nx;
+  if (!active) x0 = xlast;  // stays in the shuffles, stores nothing
+  const int nvalid = min(NPT, nx - x0);
+  const int pitch = (int)P.pitch, plane = (int)P.plane;
+  const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
+  const int r0 = y * pitch, rm = ym * pitch, rp = yp * pitch;
+  const bool first = x0 == 0;
+  const bool last = x0 == xlast;
+  const int xm = first ? nx - 1 : x0 - 1;
+  const int xp = x0 + NPT >= nx ? 0 : x0 + NPT;
+  const T* pin = static_cast<const T*>(pop_in_v);
+
+  R f[9][NPT];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const int row = cy(i) == 1 ? rm : (cy(i) == -1 ? rp : r0);
+    const T* base = pin + i * plane + row;
+    T raw[NPT];
+    ld_vec<T, NPT>(base + x0, raw);
+    R v[NPT];
+#pragma unroll
+    for (int k = 0; k < NPT; ++k) v[k] = St::to_r(raw[k], i);
+    if (cx(i) == 0) {
+#pragma unroll
+      for (int k = 0; k < NPT; ++k) f[i][k] = v[k];
+    } else if (cx(i) == 1) {
+      R prev = __shfl_up_sync(0xffffffffu, v[NPT - 1], 1);
+      if (lane == 0 || first) prev = St::ld(base + xm, i);
+      f[i][0] = prev;
+#pragma unroll
+      for (int k = 1; k < NPT; ++k) f[i][k] = v[k - 1];
+    } else {
+      R next = __shfl_down_sync(0xffffffffu, v[0], 1);
+      if (lane == 31 || last) next = St::ld(base + xp, i);
+#pragma unroll
+      for (int k = 0; k < NPT - 1; ++k) f[i][k] = v[k + 1];
+      f[i][NPT - 1] = next;
+      if (nvalid < NPT) {
+        // partial chunk: gather node by node, node nx-1 wraps to x = 0
+#pragma unroll
+        for (int k = 0; k < NPT; ++k) {
+          const int xs = x0 + k + 1 < nx ? x0 + k + 1 : 0;
+          f[i][k] = St::ld(base + xs, i);
+        }
+      }
+    }
+  }
+
+  if (HAS_BC && P.g.bcmask != nullptr) {
+    const uint32_t word = __ldg(P.g.bcmask + y * P.g.words + (x0 >> 5));
+    const uint32_t bits = (word >> (x0 & 31)) & ((NPT >= 32) ? 0xffffffffu : ((1u << NPT) - 1u));
+    if (bits) {
+      const R* aux_in = static_cast<const R*>(aux_in_v);
+#pragma unroll
+      for (int k = 0; k < NPT; ++k) {
+        if (!((bits >> k) & 1u)) continue;
+        const int x = x0 + k;
+        const uint32_t d = __ldg(P.g.desc + y * nx + x);
+        const int ks = (d >> LBM_DESC_KSET_SHIFT) & 15, cs = (d >> LBM_DESC_CSET_SHIFT) & 15;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+          const uint32_t s = (d >> (2 * i)) & 3u;
+          if (s == LBM_SRC_BOUNCE)
+            f[i][k] = St::ld(pin + opp(i) * plane + r0 + x, opp(i)) - (R)P.g.kconst[ks][i];
+          else if (s == LBM_SRC_CONST)
+            f[i][k] = (R)P.g.cconst[cs][i];
+          else if (s == LBM_SRC_OUTLET && outlet_slot(i) >= 0 && aux_in != nullptr)
+            f[i][k] = aux_in[outlet_slot(i) * ny + y];
+        }
+      }
+    }
+  }
+
+  if (aux_out_v != nullptr && active && x0 <= nx - 2 && nx - 2 < x0 + NPT) {
+    R* aux_out = static_cast<R*>(aux_out_v);
+    const int ka = nx - 2 - x0;
+    R a3 = f[3][0], a6 = f[6][0], a7 = f[7][0];
+#pragma unroll
+    for (int k = 1; k < NPT; ++k) {
+      a3 = k == ka ? f[3][k] : a3;
+      a6 = k == ka ? f[6][k] : a6;
+      a7 = k == ka ? f[7][k] : a7;
+    }
+    aux_out[0 * ny + y] = a3;
+    aux_out[1 * ny + y] = a6;
+    aux_out[2 * ny + y] = a7;
+  }
+
+  R pv[9];  // pressure rewrite computed by the node at column nx-2 or 1
+  int pcol = -1;
+  const R omega = (R)P.omega;
+#pragma unroll
+  for (int k = 0; k < NPT; ++k) {
+    R g[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) g[i] = f[i][k];
+    const R rho = density9(g);
+    R ux, uy;
+    velocity_fast(g, rho, ux, uy);
+    if (active && k < nvalid) {
+      const int x = x0 + k;
+      if (P.rho_out.p != nullptr) {
+        P.rho_out.p[x * P.rho_out.sx + y * P.rho_out.sy] = (double)rho;
+        double* up = P.u_out.p + x * P.u_out.sx + y * P.u_out.sy;
+        up[0] = (double)ux;
+        up[P.u_out.sc] = (double)uy;
+      }
+      write_probe(P, x, y, ux, uy);
+    }
+    collide_fast(g, rho, ux, uy, omega);
+    if (HAS_PRESSURE && P.g.pressure) {
+      const int x = x0 + k;
+      if (k < nvalid && (x == nx - 2 || x == 1)) {
+        R br[9];
+        bracket9_fast(ux, uy, br);
+        const R rb = (R)(x == nx - 2 ? P.g.rho_in : P.g.rho_out) - rho;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) pv[i] = fma(wr<R>(i) * br[i], rb, g[i]);
+        pcol = x;
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) f[i][k] = g[i];
+  }
+
+  if (!active) return;
+  T* pout = static_cast<T*>(pop_out_v);
+  const bool pr = HAS_PRESSURE && P.g.pressure;
+  if (nvalid == NPT && !(pr && (first || last))) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      T raw[NPT];
+#pragma unroll
+      for (int k = 0; k < NPT; ++k) raw[k] = St::from_r(f[i][k], i);
+      st_vec<T, NPT>(pout + i * plane + r0 + x0, raw);
+    }
+  } else {
+    // partial chunk, or a row end under the pressure rewrite: column 0 skips the
+    // inlet-side directions, column nx-1 the outlet side
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+#pragma unroll
+      for (int k = 0; k < NPT; ++k) {
+        const int x = x0 + k;
+        const bool skip = k >= nvalid || (pr && ((x == 0 && ((P.g.pin >> i) & 1u)) ||
+                                                 (x == nx - 1 && ((P.g.pout >> i) & 1u))));
+        if (!skip) St::st(pout + i * plane + r0 + x, f[i][k], i);
+      }
+    }
+  }
+  if (pr && pcol >= 0) {
+    const uint32_t dirs = pcol == nx - 2 ? P.g.pin : P.g.pout;
+    const int dst = pcol == nx - 2 ? 0 : nx - 1;
+#pragma unroll
+    for (int i = 0; i < 9; ++i)
+      if ((dirs >> i) & 1u) St::st(pout + i * plane + r0 + dst, pv[i], i);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched step: many lattices of different sizes advance one time step in one
+// launch.  The work is a flat list of tiles (one row segment of THREADS*NPT
+// nodes of one lattice); a persistent grid strides over it.  Lattice e is
+// live for global steps [s0, s_end); at global step g its input buffer is A
+// when (g - s0) is even.  g = *gbase + k, so a captured graph of launches
+// k = 0..K-1 followed by lbm_batch_advance stays valid across replays.
+// ---------------------------------------------------------------------------
+struct BatchEntry {
+  KParams P;
+  void* pop_a;
+  void* pop_b;
+  void* aux_a;
+  void* aux_b;
+  int xblocks;
+  int s0, s_end;
+};
+
+
+// ---- host-side checks shared by the launchers --------------------------------
+inline bool to_geok(const lbm_geometry* g, GeoK& k) {
+  if (g == nullptr) return set_error(LBM_ERR_ARG, "geometry is NULL"), false;
+  if (g->nx < 1 || g->ny < 1) return set_error(LBM_ERR_ARG, "nx and ny must be >= 1"), false;
+  if (g->bcmask != nullptr && g->desc == nullptr)
+    return set_error(LBM_ERR_ARG, "bcmask given without desc"), false;
+  if (g->n_kset < 0 || g->n_kset > LBM_MAX_SETS || g->n_cset < 0 || g->n_cset > LBM_MAX_SETS)
+    return set_error(LBM_ERR_ARG, "constant-set count out of range"), false;
+  if (g->pressure && g->nx < 2)
+    return set_error(LBM_ERR_ARG, "the pressure rewrite needs nx >= 2"), false;
+  if (g->outlet && g->nx < 2) return set_error(LBM_ERR_ARG, "the outlet needs nx >= 2"), false;
+  std::memset(&k, 0, sizeof(k));
+  k.nx = g->nx;
+  k.ny = g->ny;
+  k.words = (g->nx + 31) / 32;
+  k.bcmask = g->bcmask;
+  k.desc = g->desc;
+  k.pressure = g->pressure;
+  k.pin = g->pressure_in_dirs & 0x1FFu;
+  k.pout = g->pressure_out_dirs & 0x1FFu;
+  k.rho_in = g->rho_in;
+  k.rho_out = g->rho_out;
+  k.outlet = g->outlet;
+  std::memcpy(k.kconst, g->kconst, sizeof(k.kconst));
+  std::memcpy(k.cconst, g->cconst, sizeof(k.cconst));
+  return true;
+}
+
+inline int check_omega(double omega) {
+  if (!(omega > 0.0 && omega < 2.0)) return set_error(LBM_ERR_OMEGA, "omega must lie in (0, 2)");
+  return LBM_OK;
+}
+
+inline int check_pitch(int nx, int64_t pitch) {
+  if (pitch < nx || pitch % 8 != 0) return set_error(LBM_ERR_ARG, "pitch must be >= nx and a multiple of 8");
+  return LBM_OK;
+}
+
+inline bool v2_fits(const KParams& P, int npt) {
+  const int nx = P.g.nx;
+  if (nx < npt + 2 || P.g.ny > 65535) return false;
+  if (9 * P.plane >= ((int64_t)1 << 31) || P.pitch % npt != 0 || P.pitch < (nx + npt - 1) / npt * npt) return false;
+  if (((uintptr_t)P.pop_in | (uintptr_t)P.pop_out) % 16 != 0) return false;
+  return true;
+}
+
+
+}  // namespace lbm

@@ -16,46 +16,11 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <vector>
 
-#include "lbm_core.cuh"
-#include "lbm_host.h"
+#include "lbm_fused.cuh"
 
 namespace lbm {
-
-enum { MODE_INIT = 0, MODE_FUSED = 1, MODE_READ = 2 };
-
-struct GeoK {
-  int nx, ny, words;
-  const uint32_t* bcmask;
-  const uint32_t* desc;
-  int pressure;
-  uint32_t pin, pout;
-  double rho_in, rho_out;
-  int outlet;
-  double kconst[LBM_MAX_SETS][9];
-  double cconst[LBM_MAX_SETS][9];
-};
-
-struct View {
-  const double* p;
-  int64_t sx, sy, sc;
-};
-struct OutView {
-  double* p;
-  int64_t sx, sy, sc;
-};
-
-struct KParams {
-  GeoK g;
-  const void* pop_in;
-  void* pop_out;
-  int64_t pitch, plane;
-  const void* aux_in;
-  void* aux_out;
-  View f_in, rho_in, u_in;
-  OutView f_out, rho_out, u_out;
-  double omega;
-};
 
 template <int STORE, bool EXACT, int MODE>
 __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KParams P) {
@@ -142,6 +107,7 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
     velocity_fast(f, rho, ux, uy);
   }
 
+  if (MODE == MODE_FUSED) write_probe(P, x, y, ux, uy);
   if (MODE == MODE_READ || (MODE == MODE_FUSED && P.rho_out.p != nullptr)) {
     if (P.rho_out.p != nullptr) P.rho_out.p[x * P.rho_out.sx + y * P.rho_out.sy] = (double)rho;
     if (P.u_out.p != nullptr) {
@@ -211,197 +177,15 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
   }
 }
 
-// ---------------------------------------------------------------------------
-// Vectorised fused step.  Each thread owns NPT consecutive nodes of one row
-// (one aligned vector per population plane).  The six planes with cx = +-1
-// need the chunk shifted by one node: the missing element comes from the
-// neighbouring lane by a warp shuffle, or by a direct load at the first and
-// last lane of a warp and at the row ends (periodic wrap).  Offsets are 32-bit
-// element indices (9 * plane < 2^31).  Boundary descriptors and the pressure
-// rewrite are compiled in only for geometries that have them.
-// ---------------------------------------------------------------------------
-constexpr int kV2Threads = 128;
-
-template <int STORE, int NPT, bool HAS_BC, bool HAS_PRESSURE>
-__global__ void __launch_bounds__(kV2Threads) fused_v2_kernel(const __grid_constant__ KParams P) {
-  using St = Store<STORE>;
-  using T = typename St::T;
-  using R = typename St::R;
-  const int lane = threadIdx.x & 31;
-  const int nx = P.g.nx, ny = P.g.ny;
-  const int y = blockIdx.y;
-  int x0 = (blockIdx.x * kV2Threads + threadIdx.x) * NPT;
-  const bool active = x0 < nx;
-  if (!active) x0 = nx - NPT;  // stays in the shuffles, stores nothing
-  const int pitch = (int)P.pitch, plane = (int)P.plane;
-  const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
-  const int r0 = y * pitch, rm = ym * pitch, rp = yp * pitch;
-  const bool first = x0 == 0;
-  const bool last = x0 + NPT >= nx;
-  const int xm = first ? nx - 1 : x0 - 1;
-  const int xp = last ? 0 : x0 + NPT;
-  const T* pin = static_cast<const T*>(P.pop_in);
-
-  R f[9][NPT];
-#pragma unroll
-  for (int i = 0; i < 9; ++i) {
-    const int row = cy(i) == 1 ? rm : (cy(i) == -1 ? rp : r0);
-    const T* base = pin + i * plane + row;
-    T raw[NPT];
-    ld_vec<T, NPT>(base + x0, raw);
-    R v[NPT];
-#pragma unroll
-    for (int k = 0; k < NPT; ++k) v[k] = St::to_r(raw[k], i);
-    if (cx(i) == 0) {
-#pragma unroll
-      for (int k = 0; k < NPT; ++k) f[i][k] = v[k];
-    } else if (cx(i) == 1) {
-      R prev = __shfl_up_sync(0xffffffffu, v[NPT - 1], 1);
-      if (lane == 0 || first) prev = St::ld(base + xm, i);
-      f[i][0] = prev;
-#pragma unroll
-      for (int k = 1; k < NPT; ++k) f[i][k] = v[k - 1];
-    } else {
-      R next = __shfl_down_sync(0xffffffffu, v[0], 1);
-      if (lane == 31 || last) next = St::ld(base + xp, i);
-#pragma unroll
-      for (int k = 0; k < NPT - 1; ++k) f[i][k] = v[k + 1];
-      f[i][NPT - 1] = next;
-    }
-  }
-
-  if (HAS_BC) {
-    const uint32_t word = __ldg(P.g.bcmask + y * P.g.words + (x0 >> 5));
-    const uint32_t bits = (word >> (x0 & 31)) & ((NPT >= 32) ? 0xffffffffu : ((1u << NPT) - 1u));
-    if (bits) {
-      const R* aux_in = static_cast<const R*>(P.aux_in);
-#pragma unroll
-      for (int k = 0; k < NPT; ++k) {
-        if (!((bits >> k) & 1u)) continue;
-        const int x = x0 + k;
-        const uint32_t d = __ldg(P.g.desc + y * nx + x);
-        const int ks = (d >> LBM_DESC_KSET_SHIFT) & 15, cs = (d >> LBM_DESC_CSET_SHIFT) & 15;
-#pragma unroll
-        for (int i = 0; i < 9; ++i) {
-          const uint32_t s = (d >> (2 * i)) & 3u;
-          if (s == LBM_SRC_BOUNCE)
-            f[i][k] = St::ld(pin + opp(i) * plane + r0 + x, opp(i)) - (R)P.g.kconst[ks][i];
-          else if (s == LBM_SRC_CONST)
-            f[i][k] = (R)P.g.cconst[cs][i];
-          else if (s == LBM_SRC_OUTLET && outlet_slot(i) >= 0 && aux_in != nullptr)
-            f[i][k] = aux_in[outlet_slot(i) * ny + y];
-        }
-      }
-    }
-  }
-
-  if (P.aux_out != nullptr && x0 <= nx - 2 && nx - 2 < x0 + NPT && active) {
-    R* aux_out = static_cast<R*>(P.aux_out);
-    const int k = nx - 2 - x0;
-#pragma unroll
-    for (int kk = 0; kk < NPT; ++kk)
-      if (kk == k) {
-        aux_out[0 * ny + y] = f[3][kk];
-        aux_out[1 * ny + y] = f[6][kk];
-        aux_out[2 * ny + y] = f[7][kk];
-      }
-  }
-
-  R pv[9];  // pressure rewrite computed by the node at column nx-2 or 1
-  int pcol = -1;
-  const R omega = (R)P.omega;
-#pragma unroll
-  for (int k = 0; k < NPT; ++k) {
-    R g[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) g[i] = f[i][k];
-    const R rho = density9(g);
-    R ux, uy;
-    velocity_fast(g, rho, ux, uy);
-    if (P.rho_out.p != nullptr && active) {
-      const int x = x0 + k;
-      P.rho_out.p[x * P.rho_out.sx + y * P.rho_out.sy] = (double)rho;
-      double* up = P.u_out.p + x * P.u_out.sx + y * P.u_out.sy;
-      up[0] = (double)ux;
-      up[P.u_out.sc] = (double)uy;
-    }
-    collide_fast(g, rho, ux, uy, omega);
-    if (HAS_PRESSURE) {
-      const int x = x0 + k;
-      if (x == nx - 2 || x == 1) {
-        R br[9];
-        bracket9_fast(ux, uy, br);
-        const R rb = (R)(x == nx - 2 ? P.g.rho_in : P.g.rho_out) - rho;
-#pragma unroll
-        for (int i = 0; i < 9; ++i) pv[i] = fma(wr<R>(i) * br[i], rb, g[i]);
-        pcol = x;
-      }
-    }
-#pragma unroll
-    for (int i = 0; i < 9; ++i) f[i][k] = g[i];
-  }
-
-  if (!active) return;
-  T* pout = static_cast<T*>(P.pop_out);
-  if (!HAS_PRESSURE || !(first || last)) {
-#pragma unroll
-    for (int i = 0; i < 9; ++i) {
-      T raw[NPT];
-#pragma unroll
-      for (int k = 0; k < NPT; ++k) raw[k] = St::from_r(f[i][k], i);
-      st_vec<T, NPT>(pout + i * plane + r0 + x0, raw);
-    }
-  } else {
-    // row ends: column 0 skips the inlet-side directions, column nx-1 the outlet side
-#pragma unroll
-    for (int i = 0; i < 9; ++i) {
-#pragma unroll
-      for (int k = 0; k < NPT; ++k) {
-        const int x = x0 + k;
-        const bool skip = (x == 0 && ((P.g.pin >> i) & 1u)) || (x == nx - 1 && ((P.g.pout >> i) & 1u));
-        if (!skip) St::st(pout + i * plane + r0 + x, f[i][k], i);
-      }
-    }
-  }
-  if (HAS_PRESSURE && pcol >= 0) {
-    const uint32_t dirs = pcol == nx - 2 ? P.g.pin : P.g.pout;
-    const int dst = pcol == nx - 2 ? 0 : nx - 1;
-#pragma unroll
-    for (int i = 0; i < 9; ++i)
-      if ((dirs >> i) & 1u) St::st(pout + i * plane + r0 + dst, pv[i], i);
-  }
+template <int STORE, int NPT, int THREADS, bool HAS_BC, bool HAS_PRESSURE>
+__global__ void __launch_bounds__(THREADS) fused_v2_kernel(const __grid_constant__ KParams P) {
+  fused_v2_body<STORE, NPT, HAS_BC, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out,
+                                                  (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y);
 }
 
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-static bool to_geok(const lbm_geometry* g, GeoK& k) {
-  if (g == nullptr) return set_error(LBM_ERR_ARG, "geometry is NULL"), false;
-  if (g->nx < 1 || g->ny < 1) return set_error(LBM_ERR_ARG, "nx and ny must be >= 1"), false;
-  if (g->bcmask != nullptr && g->desc == nullptr)
-    return set_error(LBM_ERR_ARG, "bcmask given without desc"), false;
-  if (g->n_kset < 0 || g->n_kset > LBM_MAX_SETS || g->n_cset < 0 || g->n_cset > LBM_MAX_SETS)
-    return set_error(LBM_ERR_ARG, "constant-set count out of range"), false;
-  if (g->pressure && g->nx < 2)
-    return set_error(LBM_ERR_ARG, "the pressure rewrite needs nx >= 2"), false;
-  if (g->outlet && g->nx < 2) return set_error(LBM_ERR_ARG, "the outlet needs nx >= 2"), false;
-  std::memset(&k, 0, sizeof(k));
-  k.nx = g->nx;
-  k.ny = g->ny;
-  k.words = (g->nx + 31) / 32;
-  k.bcmask = g->bcmask;
-  k.desc = g->desc;
-  k.pressure = g->pressure;
-  k.pin = g->pressure_in_dirs & 0x1FFu;
-  k.pout = g->pressure_out_dirs & 0x1FFu;
-  k.rho_in = g->rho_in;
-  k.rho_out = g->rho_out;
-  k.outlet = g->outlet;
-  std::memcpy(k.kconst, g->kconst, sizeof(k.kconst));
-  std::memcpy(k.cconst, g->cconst, sizeof(k.cconst));
-  return true;
-}
-
 static void launch_dims(int nx, int ny, dim3& grid, dim3& block) {
   int bx = nx >= 128 ? 128 : ((nx + 31) / 32) * 32;
   int by = std::max(1, 128 / bx);
@@ -432,18 +216,21 @@ static int dispatch(int storage, bool exact, const KParams& P, cudaStream_t s) {
   }
 }
 
+constexpr int kV2Threads = 128;
+
 template <int STORE, int NPT>
 static int launch_v2(const KParams& P, cudaStream_t s) {
-  const dim3 grid((unsigned)((P.g.nx / NPT + kV2Threads - 1) / kV2Threads), (unsigned)P.g.ny, 1);
+  const int chunks = (P.g.nx + NPT - 1) / NPT;
+  const dim3 grid((unsigned)((chunks + kV2Threads - 1) / kV2Threads), (unsigned)P.g.ny, 1);
   const bool bc = P.g.bcmask != nullptr, pr = P.g.pressure != 0;
   if (bc && pr)
-    fused_v2_kernel<STORE, NPT, true, true><<<grid, kV2Threads, 0, s>>>(P);
+    fused_v2_kernel<STORE, NPT, kV2Threads, true, true><<<grid, kV2Threads, 0, s>>>(P);
   else if (bc)
-    fused_v2_kernel<STORE, NPT, true, false><<<grid, kV2Threads, 0, s>>>(P);
+    fused_v2_kernel<STORE, NPT, kV2Threads, true, false><<<grid, kV2Threads, 0, s>>>(P);
   else if (pr)
-    fused_v2_kernel<STORE, NPT, false, true><<<grid, kV2Threads, 0, s>>>(P);
+    fused_v2_kernel<STORE, NPT, kV2Threads, false, true><<<grid, kV2Threads, 0, s>>>(P);
   else
-    fused_v2_kernel<STORE, NPT, false, false><<<grid, kV2Threads, 0, s>>>(P);
+    fused_v2_kernel<STORE, NPT, kV2Threads, false, false><<<grid, kV2Threads, 0, s>>>(P);
   count_launch();
   return check_launch("fused_v2_kernel");
 }
@@ -452,7 +239,7 @@ static int default_npt(int storage) {
   switch (storage) {
     case LBM_STORE_F64: return 2;
     case LBM_STORE_F32: return 4;
-    default: return 8;
+    default: return 4;
   }
 }
 
@@ -461,10 +248,7 @@ static int v2_npt(int storage, int flags, const KParams& P) {
   if ((flags & LBM_FLAG_EXACT) || (flags & LBM_FLAG_GENERIC)) return 0;
   int npt = (flags >> LBM_FLAG_NPT_SHIFT) & 15;
   if (npt == 0) npt = default_npt(storage);
-  const int nx = P.g.nx;
-  if (nx % npt != 0 || nx < 2 * npt || P.g.ny > 65535) return 0;
-  if (9 * P.plane >= ((int64_t)1 << 31) || P.pitch % npt != 0) return 0;
-  if (((uintptr_t)P.pop_in | (uintptr_t)P.pop_out) % 16 != 0) return 0;
+  if (!v2_fits(P, npt)) return 0;
   return npt;
 }
 
@@ -475,8 +259,10 @@ static int launch_fused(int storage, int flags, const KParams& P, cudaStream_t s
     case LBM_STORE_F64 * 16 + 4: return launch_v2<LBM_STORE_F64, 4>(P, s);
     case LBM_STORE_F32 * 16 + 2: return launch_v2<LBM_STORE_F32, 2>(P, s);
     case LBM_STORE_F32 * 16 + 4: return launch_v2<LBM_STORE_F32, 4>(P, s);
+    case LBM_STORE_F16S * 16 + 2: return launch_v2<LBM_STORE_F16S, 2>(P, s);
     case LBM_STORE_F16S * 16 + 4: return launch_v2<LBM_STORE_F16S, 4>(P, s);
     case LBM_STORE_F16S * 16 + 8: return launch_v2<LBM_STORE_F16S, 8>(P, s);
+    case LBM_STORE_BF16S * 16 + 2: return launch_v2<LBM_STORE_BF16S, 2>(P, s);
     case LBM_STORE_BF16S * 16 + 4: return launch_v2<LBM_STORE_BF16S, 4>(P, s);
     case LBM_STORE_BF16S * 16 + 8: return launch_v2<LBM_STORE_BF16S, 8>(P, s);
     default: return dispatch<MODE_FUSED>(storage, flags & LBM_FLAG_EXACT, P, s);
@@ -499,16 +285,6 @@ static View ref_u(const double* p, int ny) { return View{p, 2LL * ny, 2, 1}; }
 static OutView ref_f_out(double* p, int ny) { return OutView{p, 9LL * ny, 9, 1}; }
 static OutView ref_rho_out(double* p, int ny) { return OutView{p, (int64_t)ny, 1, 0}; }
 static OutView ref_u_out(double* p, int ny) { return OutView{p, 2LL * ny, 2, 1}; }
-
-static int check_omega(double omega) {
-  if (!(omega > 0.0 && omega < 2.0)) return set_error(LBM_ERR_OMEGA, "omega must lie in (0, 2)");
-  return LBM_OK;
-}
-
-static int check_pitch(int nx, int64_t pitch) {
-  if (pitch < nx || pitch % 8 != 0) return set_error(LBM_ERR_ARG, "pitch must be >= nx and a multiple of 8");
-  return LBM_OK;
-}
 
 }  // namespace lbm
 
@@ -623,5 +399,6 @@ int lbm_step_f64(const lbm_geometry* g, const double* f, const double* rho, cons
   return (flags & LBM_FLAG_EXACT) ? launch<LBM_STORE_F64, true, MODE_READ>(P, (cudaStream_t)stream)
                                   : launch<LBM_STORE_F64, false, MODE_READ>(P, (cudaStream_t)stream);
 }
+
 
 }  // extern "C"

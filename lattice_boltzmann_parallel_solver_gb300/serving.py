@@ -1,0 +1,174 @@
+"""Continuous-batching serving loop for lattice solves.
+
+Requests (a boundary composition, an initial state and a step budget) arrive
+over time.  At every tick the engine admits waiting requests while their
+device state fits the HBM budget and a slot is free, advances every live
+request together by up to ``tick_steps`` steps in batched launches (one
+launch per step covering all of them), and retires the requests whose budget
+is spent: their final moments are read back and their memory is freed.
+Requests that arrive while others are on the GPU join at the next tick, so
+their work overlaps on the device.  A request's result does not depend on
+what it shared the GPU with: every lattice is updated by the same kernel and
+arithmetic whatever else is in the batch.
+"""
+from __future__ import annotations
+
+import math
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import boundary_utils as BU
+from . import scenarios as S
+from .batch import Batch, Member
+
+
+@dataclass
+class Request:
+    rid: int
+    kind: str
+    nx: int
+    ny: int
+    omega: float
+    steps: int
+    boundary: object
+    f0: np.ndarray
+    rho0: np.ndarray
+    u0: np.ndarray
+    arrival: float = 0.0          # seconds after the stream starts
+    params: dict = field(default_factory=dict)
+    # filled in by the engine
+    admitted: float = None
+    finished: float = None
+    rho: torch.Tensor = None
+    u: torch.Tensor = None
+
+    @property
+    def latency(self):
+        return None if self.finished is None else self.finished - self.arrival
+
+    @property
+    def nodes(self):
+        return self.nx * self.ny
+
+
+def request_mix(n, rate=50.0, seed=7, step_range=(1000, 50000), kinds=("couette", "poiseuille", "von_karman")):
+    """Seeded Poisson arrivals (mean ``rate`` per second) of mixed requests:
+    Couette (moving top wall u_w in [0.01, 0.1], ny in [32, 512], nx = ny),
+    pressure-driven Poiseuille (delta rho log-uniform in [1e-4, 1e-2], nx x ny
+    up to 2048 x 512) and the von Karman channel (420 x 180, Re 100)."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for rid in range(n):
+        t += rng.exponential(1.0 / rate)
+        kind = kinds[int(rng.integers(0, len(kinds)))]
+        steps = int(rng.integers(step_range[0], step_range[1] + 1))
+        if kind == "couette":
+            ny = int(rng.integers(32, 513))
+            nx = ny
+            uw = float(rng.uniform(0.01, 0.1))
+            rho, u = np.ones((nx, ny)), np.zeros((nx, ny, 2))
+            bnd = BU.Boundary([BU.rigid_wall(_row(nx, ny, 0)),
+                               BU.moving_wall(_row(nx, ny, -1), np.array([uw, 0.0]), 1.0)])
+            req = Request(rid, kind, nx, ny, 1.0, steps, bnd, S.equilibrium_np(rho, u), rho, u, t, {"u_w": uw})
+        elif kind == "poiseuille":
+            nx = int(rng.integers(64, 2049))
+            ny = int(rng.integers(16, 513))
+            drho = float(math.exp(rng.uniform(math.log(1e-4), math.log(1e-2))))
+            p_in, p_out = (1 + drho / 2) / 3, (1 - drho / 2) / 3
+            rho, u = np.ones((nx, ny)), np.zeros((nx, ny, 2))
+            bnd = BU.poiseuille_flow_boundary_conditions(nx, ny, p_in, p_out)
+            req = Request(rid, kind, nx, ny, 1.5, steps, bnd, S.equilibrium_np(rho, u), rho, u, t, {"drho": drho})
+        else:
+            f, rho, u, om, bnd = S.von_karman(420, 180, plate=40, re=100, seed=rid)
+            req = Request(rid, kind, 420, 180, om, steps, bnd, f, rho, u, t, {"re": 100})
+        out.append(req)
+    return out
+
+
+def _row(nx, ny, y):
+    m = np.zeros((nx, ny), dtype=bool)
+    m[:, y] = True
+    return m
+
+
+class ServingEngine:
+    """Admits, batches and retires lattice solves on one GPU."""
+
+    def __init__(self, storage="f16", hbm_budget=64 << 30, max_slots=128, tick_steps=500, npt=0, threads=128,
+                 blocks=0, device="cuda"):
+        self.storage = storage
+        self.hbm_budget = int(hbm_budget)
+        self.max_slots = max_slots
+        self.tick_steps = tick_steps
+        self.batch = Batch([], storage=storage, npt=npt, threads=threads, blocks=blocks, device=device)
+        self.live = []          # (Request, Member)
+        self.used = 0
+        self.stats = {"ticks": 0, "max_live": 0, "steps": 0}
+
+    def state_bytes(self, req):
+        per = {"f64": 8, "f32": 4, "f16": 2, "bf16": 2}[self.storage]
+        pitch = (req.nx + 31) // 32 * 32
+        return 2 * 9 * req.ny * pitch * per + 2 * 3 * req.ny * 8
+
+    def serve(self, requests, realtime=True):
+        """Run an arrival stream to completion.  With ``realtime`` the arrival
+        times are wall-clock offsets from the start; otherwise every request is
+        waiting from the start (a closed loop).  Returns the finished requests
+        with timings and results (rho, u on the device) filled in."""
+        pending = sorted(requests, key=lambda r: r.arrival)
+        waiting, done = [], []
+        b = self.batch
+        t0 = time.perf_counter()
+        i = 0
+        while i < len(pending) or waiting or self.live:
+            now = time.perf_counter() - t0
+            if not waiting and not self.live and i < len(pending) and realtime and pending[i].arrival > now:
+                time.sleep(pending[i].arrival - now)
+                now = time.perf_counter() - t0
+            while i < len(pending) and (pending[i].arrival <= now or not realtime):
+                waiting.append(pending[i])
+                i += 1
+            while waiting and len(self.live) < self.max_slots and \
+                    self.used + self.state_bytes(waiting[0]) <= self.hbm_budget:
+                r = waiting.pop(0)
+                r.admitted = now
+                m = b.add(Member(r.nx, r.ny, r.omega, r.boundary, steps=r.steps, f0=r.f0, rho0=r.rho0, u0=r.u0))
+                self.live.append((r, m))
+                self.used += self.state_bytes(r)
+            if not self.live:
+                if waiting:
+                    raise RuntimeError("request %d does not fit the HBM budget" % waiting[0].rid)
+                continue
+            left = min(m.s0 + m.steps - 1 - b.g for _, m in self.live)
+            n = max(0, min(self.tick_steps, left))
+            b.run(n)
+            self.stats["ticks"] += 1
+            self.stats["steps"] += n
+            self.stats["max_live"] = max(self.stats["max_live"], len(self.live))
+            finished = [(r, m) for r, m in self.live if b.done(m)]
+            if finished:
+                for r, m in finished:
+                    _, r.rho, r.u = b.read(m, want_f=False)
+                torch.cuda.synchronize()
+                now = time.perf_counter() - t0
+                for r, m in finished:
+                    r.finished = now
+                    self.used -= self.state_bytes(r)
+                    b.remove(m)
+                    done.append(r)
+                ids = {id(m) for _, m in finished}
+                self.live = [(r, m) for r, m in self.live if id(m) not in ids]
+        return done
+
+
+def summarize(done):
+    lat = np.array([r.latency for r in done])
+    span = max(r.finished for r in done) - min(r.arrival for r in done)
+    nodes_steps = sum(r.nodes * r.steps for r in done)
+    return {"requests": len(done), "solves_per_s": len(done) / span, "p50_s": float(np.percentile(lat, 50)),
+            "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()), "span_s": span,
+            "mlups": nodes_steps / span / 1e6}

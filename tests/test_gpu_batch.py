@@ -1,0 +1,103 @@
+"""Batched lattices (one launch per step over many uneven lattices): each
+member's result equals the same lattice run alone, float64 members match the
+oracle, per-lattice step budgets stop on time, graph replay equals plain
+launches, probes record the per-step velocity, and the autotuner returns a
+working configuration."""
+import numpy as np
+import pytest
+import torch
+
+from oracle import lbm_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pkg():
+    import lattice_boltzmann_parallel_solver_gb300 as P
+    P._lib.load()
+    return P
+
+
+def members(pkg, steps=(30, 30, 30, 30, 30)):
+    S, U = pkg.scenarios, pkg.boundary_utils
+    from lattice_boltzmann_parallel_solver_gb300.batch import Member
+    out = []
+    f, rho, u, om, bnd = S.von_karman(203, 62, plate=12, re=120, seed=1)
+    out.append(Member(203, 62, om, bnd, steps=steps[0], f0=f, rho0=rho, u0=u, probe=(150, 31)))
+    f, rho, u, om, bnd = S.von_karman(96, 40, plate=8, re=60, seed=2, plate_offset=0, walls=False)
+    out.append(Member(96, 40, om, bnd, steps=steps[1], f0=f, rho0=rho, u0=u))
+    f, rho, u, bnd = S.cavity(37)
+    out.append(Member(37, 37, 1.7, bnd, steps=steps[2], f0=f, rho0=rho, u0=u))
+    rho, u = np.ones((50, 18)), np.zeros((50, 18, 2))
+    out.append(Member(50, 18, 1.5, U.poiseuille_flow_boundary_conditions(50, 18, (1 + 3e-3) / 3, (1 - 3e-3) / 3),
+                      steps=steps[3], f0=S.equilibrium_np(rho, u), rho0=rho, u0=u))
+    f, rho, u = S.shear_wave(64)
+    out.append(Member(64, 64, 1.0, None, steps=steps[4], f0=f, rho0=rho, u0=u))
+    return out
+
+
+def alone(pkg, m, storage, npt):
+    lat = pkg.Lattice(m.nx, m.ny, m.omega, m.boundary, storage=storage, npt=npt)
+    return lat.set_state(m.f0, m.rho0, m.u0).step(m.steps)
+
+
+@pytest.mark.parametrize("storage,npt,threads", [("f64", 2, 128), ("f32", 4, 64), ("f16", 4, 128),
+                                                 ("f16", 8, 256), ("bf16", 2, 128)])
+def test_batch_members_equal_lone_runs(pkg, storage, npt, threads):
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch
+    ms = members(pkg, steps=(30, 17, 25, 30, 4))
+    b = Batch(ms, storage=storage, npt=npt, threads=threads).start()
+    b.run()
+    for j, m in enumerate(ms):
+        got = b.read(j)[0]
+        ref = alone(pkg, m, storage, npt).read()[0]
+        err = float((got - ref).abs().max() / ref.abs().max())
+        assert err <= (1e-13 if storage == "f64" else 1e-6), (j, err)
+
+
+def test_batch_f64_against_oracle(pkg):
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch
+    ms = members(pkg)
+    b = Batch(ms, storage="f64").start()
+    b.run()
+    cav = ms[2]
+    ref = O.run(cav.f0, cav.rho0, cav.u0, 1.7, cav.steps, O.cavity_boundary(37, 37, 0.1, 1.0))
+    got = b.read(2)[0].cpu().numpy()
+    assert np.abs(got - ref[0]).max() / np.abs(ref[0]).max() <= 1e-12
+    she = ms[4]
+    ref = O.run(she.f0, she.rho0, she.u0, 1.0, she.steps)
+    got = b.read(4)[0].cpu().numpy()
+    assert np.abs(got - ref[0]).max() / np.abs(ref[0]).max() <= 1e-12
+
+
+def test_graph_replay_and_probe(pkg):
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch
+    ms = members(pkg, steps=(241, 241, 241, 241, 241))
+    a = Batch(ms, storage="f32").start()
+    a.run()
+    ms2 = members(pkg, steps=(241, 241, 241, 241, 241))
+    b = Batch(ms2, storage="f32").start()
+    b.run_graph(chunk=40)
+    for j in range(len(ms)):
+        assert torch.equal(a.read(j)[0], b.read(j)[0])
+    tr = b.probe_trace(0)
+    assert tr.shape == (240, 2)
+    # the last recorded probe is the velocity of the last step's pre-collision state,
+    # i.e. of the state one step before the final one
+    m = ms2[0]
+    lat = pkg.Lattice(m.nx, m.ny, m.omega, m.boundary, storage="f32").set_state(m.f0, m.rho0, m.u0).step(240)
+    u = lat.moments()[1][150, 31]
+    assert torch.allclose(tr[-1], u.to(tr.dtype), rtol=0, atol=1e-6)
+
+
+def test_autotune_picks_a_working_config(pkg):
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch, autotune
+    ms = members(pkg, steps=(20, 20, 20, 20, 20))
+    b = Batch(ms, storage="f16")
+    res = autotune(b, steps=3, warmup=1)
+    assert res and all(r["ms_per_step"] > 0 for r in res)
+    b.start().run()
+    for j, m in enumerate(ms):
+        ref = alone(pkg, m, "f16", b.npt).read()[0]
+        assert float((b.read(j)[0] - ref).abs().max()) <= 1e-6
