@@ -77,6 +77,7 @@ typedef struct lbm_geometry {
 #define LBM_FLAG_EXACT 1  /* float64 arithmetic in the reference's NumPy operation order, no FMA contraction */
 #define LBM_FLAG_GENERIC 2 /* use the one-node-per-thread kernel instead of the vectorised one */
 #define LBM_FLAG_NPT_SHIFT 4 /* bits 4..7: nodes per thread of the vectorised kernel (0 = default) */
+#define LBM_FLAG_STOCHASTIC 256 /* 16-bit storages: round stored deviations stochastically */
 
 /* ---- library ------------------------------------------------------------ */
 int lbm_version(void);
@@ -151,10 +152,12 @@ int lbm_lattice_init(const lbm_geometry* g, int32_t storage, const double* f, co
  * (pop_a, aux_a) and (pop_b, aux_b), starting from pop_a.  After an odd
  * number of steps the state is in pop_b.  When rho_out/u_out are not NULL
  * the moments of the pre-collision state of the LAST step are written as
- * SoA planes rho[ny][pitch], u[2][ny][pitch] (float64). */
+ * SoA planes rho[ny][pitch], u[2][ny][pitch] (float64).  With LBM_FLAG_STOCHASTIC
+ * the 16-bit storages round their stored deviations stochastically; step s of
+ * the call draws its random bits from (seed, s, node, direction). */
 int lbm_lattice_run(const lbm_geometry* g, int32_t storage, void* pop_a, void* pop_b, int64_t pitch,
                     void* aux_a, void* aux_b, double omega, int32_t nsteps, double* rho_out,
-                    double* u_out, int32_t flags, void* stream);
+                    double* u_out, int32_t flags, uint32_t seed, void* stream);
 /* Materialise the current (post-streaming, post-boundary) state in the
  * reference layout: f_out[nx][ny][9], rho_out[nx][ny], u_out[nx][ny][2]
  * (any may be NULL). */
@@ -185,6 +188,8 @@ typedef struct lbm_batch_lattice {
   int32_t probe_x, probe_y, probe_cap;
   double* probe_buf;
   int32_t* probe_count;
+  uint32_t seed;  /* stochastic rounding: random bits from (seed, g - s0, node, direction) */
+  int32_t flags;  /* LBM_FLAG_STOCHASTIC */
 } lbm_batch_lattice;
 
 size_t lbm_batch_table_bytes(int32_t n);

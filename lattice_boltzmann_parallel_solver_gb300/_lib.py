@@ -25,6 +25,7 @@ STORE_F64, STORE_F32, STORE_F16S, STORE_BF16S = 0, 1, 2, 3
 FLAG_EXACT = 1
 FLAG_GENERIC = 2
 FLAG_NPT_SHIFT = 4
+FLAG_STOCHASTIC = 256
 
 vp = C.c_void_p
 i32 = C.c_int32
@@ -53,7 +54,8 @@ class BatchLattice(C.Structure):
     """lbm_batch_lattice in include/lbm_gb300.h"""
     _fields_ = [("g", vp), ("pop_a", vp), ("pop_b", vp), ("aux_a", vp), ("aux_b", vp), ("pitch", i64),
                 ("omega", f64), ("s0", i32), ("s_end", i32), ("probe_x", i32), ("probe_y", i32),
-                ("probe_cap", i32), ("probe_buf", vp), ("probe_count", vp)]
+                ("probe_cap", i32), ("probe_buf", vp), ("probe_count", vp), ("seed", C.c_uint32),
+                ("flags", i32)]
 
 # name: (restype, argtypes)
 SIGNATURES = {
@@ -73,7 +75,7 @@ SIGNATURES = {
     "lbm_step_f64_noalloc": (C.c_int, [GP, vp, vp, vp, f64, vp, vp, vp, i32, vp]),
     "lbm_lattice_pop_bytes": (C.c_size_t, [i32, i32, i64, i32]),
     "lbm_lattice_init": (C.c_int, [GP, i32, vp, vp, vp, f64, vp, i64, vp, i32, vp]),
-    "lbm_lattice_run": (C.c_int, [GP, i32, vp, vp, i64, vp, vp, f64, i32, vp, vp, i32, vp]),
+    "lbm_lattice_run": (C.c_int, [GP, i32, vp, vp, i64, vp, vp, f64, i32, vp, vp, i32, C.c_uint32, vp]),
     "lbm_lattice_read": (C.c_int, [GP, i32, vp, i64, vp, vp, vp, vp, vp]),
     "lbm_batch_table_bytes": (C.c_size_t, [i32]),
     "lbm_batch_build": (C.c_int, [C.POINTER(BatchLattice), i32, i32, i32, vp, C.c_size_t, C.POINTER(i32), vp]),

@@ -35,6 +35,7 @@ class Member:
     f0: object = None            # reference-layout initial populations
     rho0: object = None
     u0: object = None
+    seed: int = 0                # random bits of the stochastic rounding (16-bit storages)
     # filled in by the batch
     geo: object = None
     pitch: int = 0
@@ -54,8 +55,9 @@ class Batch:
     Members can join (``add``) and leave (``remove``) between runs."""
 
     def __init__(self, members=(), storage: str = "f16", npt: int = 0, threads: int = 128, blocks: int = 0,
-                 device: str = "cuda"):
+                 device: str = "cuda", stochastic: bool = None):
         A.require_cuda()
+        self.stochastic = storage in ("f16", "bf16") if stochastic is None else bool(stochastic)
         self.storage = storage
         self.store_id, self.pop_dtype, self.aux_dtype = STORAGES[storage]
         self.device = torch.device(device)
@@ -140,6 +142,8 @@ class Batch:
                 c.probe_buf, c.probe_count = m.probe_buf.data_ptr(), m.probe_count.data_ptr()
             else:
                 c.probe_x = c.probe_y = -1
+            c.seed = int(m.seed) & 0xFFFFFFFF
+            c.flags = _lib.FLAG_STOCHASTIC if self.stochastic else 0
         size = int(_lib.load().lbm_batch_table_bytes(n))
         self.table = torch.empty(size, dtype=torch.uint8, device=self.device)
         tiles = ctypes.c_int32(0)

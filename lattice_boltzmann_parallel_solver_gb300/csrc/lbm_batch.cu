@@ -27,7 +27,8 @@ __global__ void __launch_bounds__(THREADS) batch_kernel(const BatchEntry* __rest
     const bool odd = (g - e.s0) & 1;
     fused_v2_body<STORE, NPT, true, true>(e.P, odd ? e.pop_b : e.pop_a, odd ? e.pop_a : e.pop_b,
                                           odd ? e.aux_b : e.aux_a, odd ? e.aux_a : e.aux_b,
-                                          (xb * THREADS + threadIdx.x) * NPT, y);
+                                          (xb * THREADS + threadIdx.x) * NPT, y,
+                                          hash32(e.P.seed + (uint32_t)(g - e.s0)));
   }
 }
 
@@ -74,6 +75,8 @@ int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_
     e.P.probe_cap = L.probe_cap;
     e.P.probe_buf = L.probe_buf;
     e.P.probe_count = L.probe_count;
+    e.P.seed = L.seed;
+    e.P.sr = (L.flags & LBM_FLAG_STOCHASTIC) != 0;
     if (L.probe_buf != nullptr && L.probe_count == nullptr)
       return set_error(LBM_ERR_ARG, "a probe needs its counter");
     if (!v2_fits(e.P, npt)) return set_error(LBM_ERR_UNSUPPORTED, "a batch lattice is too narrow or too large for npt");

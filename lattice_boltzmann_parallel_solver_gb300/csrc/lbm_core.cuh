@@ -42,6 +42,7 @@ template <> struct Store<LBM_STORE_F64> {
   __device__ static void st(T* p, R v, int) { *p = v; }
   __device__ static R to_r(T t, int) { return t; }
   __device__ static T from_r(R v, int) { return v; }
+  static constexpr bool kShifted = false;
 };
 template <> struct Store<LBM_STORE_F32> {
   using T = float;
@@ -50,6 +51,7 @@ template <> struct Store<LBM_STORE_F32> {
   __device__ static void st(T* p, R v, int) { *p = v; }
   __device__ static R to_r(T t, int) { return t; }
   __device__ static T from_r(R v, int) { return v; }
+  static constexpr bool kShifted = false;
 };
 // shifted storage: the deviation f_i - w_i is kept in 16 bits
 template <> struct Store<LBM_STORE_F16S> {
@@ -59,6 +61,18 @@ template <> struct Store<LBM_STORE_F16S> {
   __device__ static void st(T* p, R v, int i) { *p = __float2half_rn(v - wf(i)); }
   __device__ static R to_r(T t, int i) { return wf(i) + __half2float(t); }
   __device__ static T from_r(R v, int i) { return __float2half_rn(v - wf(i)); }
+  static constexpr bool kShifted = true;
+  __device__ static R dev(T t) { return __half2float(t); }
+  __device__ static R ld_dev(const T* p) { return __half2float(__ldg(p)); }
+  __device__ static T dev_rn(R d) { return __float2half_rn(d); }
+  // stochastic rounding with 10 random bits: add r/1024 of the binary16 ulp of
+  // |d| (2^(E-10), or 2^-24 below the normal range) away from zero, then truncate
+  __device__ static T dev_sr(R d, uint32_t r) {
+    const uint32_t e = (__float_as_uint(d) >> 23) & 0xFFu;
+    const uint32_t ulp = e >= 113u ? ((e - 10u) << 23) : (103u << 23);
+    const float noise = __uint_as_float(ulp) * ((float)(r & 0x3FFu) * 9.765625e-4f);
+    return __float2half_rz(d + copysignf(noise, d));
+  }
 };
 template <> struct Store<LBM_STORE_BF16S> {
   using T = __nv_bfloat16;
@@ -67,7 +81,27 @@ template <> struct Store<LBM_STORE_BF16S> {
   __device__ static void st(T* p, R v, int i) { *p = __float2bfloat16_rn(v - wf(i)); }
   __device__ static R to_r(T t, int i) { return wf(i) + __bfloat162float(t); }
   __device__ static T from_r(R v, int i) { return __float2bfloat16_rn(v - wf(i)); }
+  static constexpr bool kShifted = true;
+  __device__ static R dev(T t) { return __bfloat162float(t); }
+  __device__ static R ld_dev(const T* p) { return __bfloat162float(__ldg(p)); }
+  __device__ static T dev_rn(R d) { return __float2bfloat16_rn(d); }
+  // stochastic rounding with 10 random bits added below the kept 16 bits
+  __device__ static T dev_sr(R d, uint32_t r) {
+    const uint32_t u = __float_as_uint(d) + ((r & 0x3FFu) << 6);
+    return __ushort_as_bfloat16((unsigned short)(u >> 16));
+  }
 };
+
+// 32-bit integer hash (C. Wellons' "lowbias32" constants) for the random bits
+// of the stochastic rounding
+__host__ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x21f0aaadu;
+  x ^= x >> 15;
+  x *= 0x735a2d97u;
+  x ^= x >> 15;
+  return x;
+}
 
 // N contiguous elements, N * sizeof(T) bytes aligned to that size (up to 16)
 template <typename T, int N>
@@ -227,6 +261,33 @@ __device__ __forceinline__ void collide_fast(R f[9], R rho, R ux, R uy, R omega)
   LBM_PAIR(5, 7, d58, W5, V5)
   LBM_PAIR(6, 8, d67, W5, V5)
 #undef LBM_PAIR
+}
+
+// The same collision on deviations d_i = f_i - w_i (float32): with
+// drho = rho - 1 = sum d_i, d_i' = (1 - omega) d_i + omega w_i (drho + rho (4.5 cu^2 +- 3 cu - 1.5 |u|^2)).
+__device__ __forceinline__ void collide_dev(float d[9], float drho, float ux, float uy, float omega) {
+  const float rho = 1.0f + drho;
+  const float om1 = 1.0f - omega;
+  const float Bd = -1.5f * fmaf(ux, ux, uy * uy);
+  const float orho = omega * rho, odr = omega * drho;
+  const float W0 = orho * wf(0), W1 = orho * wf(1), W5 = orho * wf(5);
+  const float D0 = odr * wf(0), D1 = odr * wf(1), D5 = odr * wf(5);
+  const float V1 = 3.0f * W1, V5 = 3.0f * W5;
+  d[0] = fmaf(om1, d[0], fmaf(W0, Bd, D0));
+  const float d58 = ux + uy, d67 = uy - ux;
+#define LBM_DPAIR(I, J, V, W, D, VV)                 \
+  {                                                 \
+    const float t = fmaf(4.5f * (V), (V), Bd);      \
+    const float s = fmaf((W), t, (D));              \
+    const float m = (VV) * (V);                     \
+    d[I] = fmaf(om1, d[I], s + m);                  \
+    d[J] = fmaf(om1, d[J], s - m);                  \
+  }
+  LBM_DPAIR(1, 3, ux, W1, D1, V1)
+  LBM_DPAIR(2, 4, uy, W1, D1, V1)
+  LBM_DPAIR(5, 7, d58, W5, D5, V5)
+  LBM_DPAIR(6, 8, d67, W5, D5, V5)
+#undef LBM_DPAIR
 }
 
 // equilibrium with FMAs (used where the fast path needs feq itself)

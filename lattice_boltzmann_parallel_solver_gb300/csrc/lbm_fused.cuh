@@ -47,6 +47,11 @@ struct KParams {
   int probe_x, probe_y, probe_cap;
   double* probe_buf;
   int* probe_count;
+  // 16-bit storages: stochastic rounding of the stored deviations (sr != 0),
+  // random bits hashed from (node, direction, seed); the launcher varies the
+  // seed per step
+  uint32_t seed;
+  int sr;
 };
 
 template <typename R>
@@ -75,10 +80,13 @@ __device__ __forceinline__ void write_probe(const KParams& P, int x, int y, R ux
 // ---------------------------------------------------------------------------
 template <int STORE, int NPT, bool HAS_BC, bool HAS_PRESSURE>
 __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_in_v, void* pop_out_v,
-                                              const void* aux_in_v, void* aux_out_v, int x0, int y) {
+                                              const void* aux_in_v, void* aux_out_v, int x0, int y,
+                                              uint32_t seed) {
   using St = Store<STORE>;
   using T = typename St::T;
   using R = typename St::R;
+  // working values: deviations d = f - w for the shifted 16-bit storages, f otherwise
+  constexpr bool SH = St::kShifted;
   const int lane = threadIdx.x & 31;
   const int nx = P.g.nx, ny = P.g.ny;
   const int xlast = ((nx - 1) / NPT) * NPT;  // first node of the last chunk of a row
@@ -93,6 +101,16 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
   const int xm = first ? nx - 1 : x0 - 1;
   const int xp = x0 + NPT >= nx ? 0 : x0 + NPT;
   const T* pin = static_cast<const T*>(pop_in_v);
+  auto ld_work = [&](const T* p, int i) -> R {
+    if constexpr (SH) return St::ld_dev(p);
+    else return St::ld(p, i);
+  };
+  auto work_of_raw = [&](T t, int i) -> R {
+    if constexpr (SH) return St::dev(t);
+    else return St::to_r(t, i);
+  };
+  auto work_of_f = [&](R fv, int i) -> R { return SH ? fv - wr<R>(i) : fv; };
+  auto f_of_work = [&](R v, int i) -> R { return SH ? v + wr<R>(i) : v; };
 
   R f[9][NPT];
 #pragma unroll
@@ -103,19 +121,19 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     ld_vec<T, NPT>(base + x0, raw);
     R v[NPT];
 #pragma unroll
-    for (int k = 0; k < NPT; ++k) v[k] = St::to_r(raw[k], i);
+    for (int k = 0; k < NPT; ++k) v[k] = work_of_raw(raw[k], i);
     if (cx(i) == 0) {
 #pragma unroll
       for (int k = 0; k < NPT; ++k) f[i][k] = v[k];
     } else if (cx(i) == 1) {
       R prev = __shfl_up_sync(0xffffffffu, v[NPT - 1], 1);
-      if (lane == 0 || first) prev = St::ld(base + xm, i);
+      if (lane == 0 || first) prev = ld_work(base + xm, i);
       f[i][0] = prev;
 #pragma unroll
       for (int k = 1; k < NPT; ++k) f[i][k] = v[k - 1];
     } else {
       R next = __shfl_down_sync(0xffffffffu, v[0], 1);
-      if (lane == 31 || last) next = St::ld(base + xp, i);
+      if (lane == 31 || last) next = ld_work(base + xp, i);
 #pragma unroll
       for (int k = 0; k < NPT - 1; ++k) f[i][k] = v[k + 1];
       f[i][NPT - 1] = next;
@@ -124,7 +142,7 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
 #pragma unroll
         for (int k = 0; k < NPT; ++k) {
           const int xs = x0 + k + 1 < nx ? x0 + k + 1 : 0;
-          f[i][k] = St::ld(base + xs, i);
+          f[i][k] = ld_work(base + xs, i);
         }
       }
     }
@@ -145,17 +163,18 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
         for (int i = 0; i < 9; ++i) {
           const uint32_t s = (d >> (2 * i)) & 3u;
           if (s == LBM_SRC_BOUNCE)
-            f[i][k] = St::ld(pin + opp(i) * plane + r0 + x, opp(i)) - (R)P.g.kconst[ks][i];
+            f[i][k] = ld_work(pin + opp(i) * plane + r0 + x, opp(i)) - (R)P.g.kconst[ks][i];
           else if (s == LBM_SRC_CONST)
-            f[i][k] = (R)P.g.cconst[cs][i];
+            f[i][k] = work_of_f((R)P.g.cconst[cs][i], i);
           else if (s == LBM_SRC_OUTLET && outlet_slot(i) >= 0 && aux_in != nullptr)
-            f[i][k] = aux_in[outlet_slot(i) * ny + y];
+            f[i][k] = work_of_f(aux_in[outlet_slot(i) * ny + y], i);
         }
       }
     }
   }
 
   if (aux_out_v != nullptr && active && x0 <= nx - 2 && nx - 2 < x0 + NPT) {
+    // the outlet memory holds full populations in every kernel
     R* aux_out = static_cast<R*>(aux_out_v);
     const int ka = nx - 2 - x0;
     R a3 = f[3][0], a6 = f[6][0], a7 = f[7][0];
@@ -165,9 +184,9 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
       a6 = k == ka ? f[6][k] : a6;
       a7 = k == ka ? f[7][k] : a7;
     }
-    aux_out[0 * ny + y] = a3;
-    aux_out[1 * ny + y] = a6;
-    aux_out[2 * ny + y] = a7;
+    aux_out[0 * ny + y] = f_of_work(a3, 3);
+    aux_out[1 * ny + y] = f_of_work(a6, 6);
+    aux_out[2 * ny + y] = f_of_work(a7, 7);
   }
 
   R pv[9];  // pressure rewrite computed by the node at column nx-2 or 1
@@ -178,7 +197,8 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     R g[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) g[i] = f[i][k];
-    const R rho = density9(g);
+    const R sum = density9(g);
+    const R rho = SH ? R(1) + sum : sum;
     R ux, uy;
     velocity_fast(g, rho, ux, uy);
     if (active && k < nvalid) {
@@ -191,7 +211,8 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
       }
       write_probe(P, x, y, ux, uy);
     }
-    collide_fast(g, rho, ux, uy, omega);
+    if constexpr (SH) collide_dev(g, sum, ux, uy, omega);
+    else collide_fast(g, rho, ux, uy, omega);
     if (HAS_PRESSURE && P.g.pressure) {
       const int x = x0 + k;
       if (k < nvalid && (x == nx - 2 || x == 1)) {
@@ -208,6 +229,25 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
   }
 
   if (!active) return;
+  // working value -> stored element (stochastic rounding for 16-bit deviations)
+  const bool sr = SH && P.sr;
+  auto to_store = [&](R v, int i, uint32_t rbits) -> T {
+    if constexpr (SH) return sr ? St::dev_sr(v, rbits) : St::dev_rn(v);
+    else return St::from_r(v, i);
+  };
+  uint32_t hk[NPT][3];
+#pragma unroll
+  for (int k = 0; k < NPT; ++k) {
+    if (sr) {
+      const uint32_t h0 = hash32((uint32_t)(y * nx + x0 + k) * 0x9E3779B1u ^ seed);
+      hk[k][0] = h0;
+      hk[k][1] = hash32(h0 + 0x68E31DA4u);
+      hk[k][2] = hash32(h0 + 0xB5297A4Du);
+    } else {
+      hk[k][0] = hk[k][1] = hk[k][2] = 0u;
+    }
+  }
+#define LBM_RBITS(k, i) (hk[k][(i) / 3] >> (10 * ((i) % 3)))
   T* pout = static_cast<T*>(pop_out_v);
   const bool pr = HAS_PRESSURE && P.g.pressure;
   if (nvalid == NPT && !(pr && (first || last))) {
@@ -215,7 +255,7 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     for (int i = 0; i < 9; ++i) {
       T raw[NPT];
 #pragma unroll
-      for (int k = 0; k < NPT; ++k) raw[k] = St::from_r(f[i][k], i);
+      for (int k = 0; k < NPT; ++k) raw[k] = to_store(f[i][k], i, LBM_RBITS(k, i));
       st_vec<T, NPT>(pout + i * plane + r0 + x0, raw);
     }
   } else {
@@ -228,17 +268,19 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
         const int x = x0 + k;
         const bool skip = k >= nvalid || (pr && ((x == 0 && ((P.g.pin >> i) & 1u)) ||
                                                  (x == nx - 1 && ((P.g.pout >> i) & 1u))));
-        if (!skip) St::st(pout + i * plane + r0 + x, f[i][k], i);
+        if (!skip) pout[i * plane + r0 + x] = to_store(f[i][k], i, LBM_RBITS(k, i));
       }
     }
   }
   if (pr && pcol >= 0) {
     const uint32_t dirs = pcol == nx - 2 ? P.g.pin : P.g.pout;
     const int dst = pcol == nx - 2 ? 0 : nx - 1;
+    const uint32_t hp = sr ? hash32((uint32_t)(y * nx + dst) * 0x9E3779B1u ^ seed ^ 0x5bd1e995u) : 0u;
 #pragma unroll
     for (int i = 0; i < 9; ++i)
-      if ((dirs >> i) & 1u) St::st(pout + i * plane + r0 + dst, pv[i], i);
+      if ((dirs >> i) & 1u) pout[i * plane + r0 + dst] = to_store(pv[i], i, hp >> (3 * i));
   }
+#undef LBM_RBITS
 }
 
 // ---------------------------------------------------------------------------

@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
 template <int STORE, int NPT, int THREADS, bool HAS_BC, bool HAS_PRESSURE>
 __global__ void __launch_bounds__(THREADS) fused_v2_kernel(const __grid_constant__ KParams P) {
   fused_v2_body<STORE, NPT, HAS_BC, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out,
-                                                  (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y);
+                                                  (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y, P.seed);
 }
 
 // ---------------------------------------------------------------------------
@@ -323,7 +323,7 @@ int lbm_lattice_init(const lbm_geometry* g, int32_t storage, const double* f, co
 
 int lbm_lattice_run(const lbm_geometry* g, int32_t storage, void* pop_a, void* pop_b, int64_t pitch,
                     void* aux_a, void* aux_b, double omega, int32_t nsteps, double* rho_out,
-                    double* u_out, int32_t flags, void* stream) {
+                    double* u_out, int32_t flags, uint32_t seed, void* stream) {
   KParams P;
   std::memset(&P, 0, sizeof(P));
   if (!to_geok(g, P.g)) return last_status();
@@ -337,7 +337,9 @@ int lbm_lattice_run(const lbm_geometry* g, int32_t storage, void* pop_a, void* p
   P.pitch = pitch;
   P.plane = pitch * g->ny;
   P.omega = omega;
+  P.sr = (flags & LBM_FLAG_STOCHASTIC) != 0;
   for (int s = 0; s < nsteps; ++s) {
+    P.seed = hash32(seed + (uint32_t)s);
     const bool even = (s % 2) == 0;
     P.pop_in = even ? pop_a : pop_b;
     P.pop_out = even ? pop_b : pop_a;

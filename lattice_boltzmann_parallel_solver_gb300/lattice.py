@@ -35,9 +35,13 @@ class Lattice:
     """An nx x ny D2Q9 lattice with a fused boundary composition, resident on the device."""
 
     def __init__(self, nx: int, ny: int, omega: float, boundary=None, storage: str = "f64",
-                 exact: bool = False, device: str = "cuda", generic: bool = False, npt: int = 0):
+                 exact: bool = False, device: str = "cuda", generic: bool = False, npt: int = 0,
+                 stochastic: bool = None, seed: int = 0):
         """``generic`` forces the one-node-per-thread kernel; ``npt`` sets the
-        nodes per thread of the vectorised kernel (0 = the default for the storage)."""
+        nodes per thread of the vectorised kernel (0 = the default for the storage).
+        ``stochastic`` (default: on for the 16-bit storages) rounds the stored
+        deviations stochastically, which keeps increments smaller than half a
+        16-bit step from being lost; ``seed`` seeds its random bits."""
         A.require_cuda()
         assert 0 < omega < 2
         assert storage in STORAGES, "storage must be one of %s" % sorted(STORAGES)
@@ -45,8 +49,11 @@ class Lattice:
         self.nx, self.ny, self.omega = int(nx), int(ny), float(omega)
         self.storage = storage
         self.store_id, self.pop_dtype, self.aux_dtype = STORAGES[storage]
+        if stochastic is None:
+            stochastic = storage in ("f16", "bf16")
         self.flags = (_lib.FLAG_EXACT if exact else 0) | (_lib.FLAG_GENERIC if generic else 0) | \
-            ((int(npt) & 15) << _lib.FLAG_NPT_SHIFT)
+            ((int(npt) & 15) << _lib.FLAG_NPT_SHIFT) | (_lib.FLAG_STOCHASTIC if stochastic else 0)
+        self.seed = int(seed) & 0xFFFFFFFF
         self.pitch = (self.nx + 31) // 32 * 32
         self.device = torch.device(device)
         self.boundary = boundary
@@ -95,7 +102,8 @@ class Lattice:
         a, b = self.cur, 1 - self.cur
         _lib.call("lbm_lattice_run", self.geo.ref, self.store_id, self.pop[a].data_ptr(), self.pop[b].data_ptr(),
                   self.pitch, self.aux[a].data_ptr(), self.aux[b].data_ptr(), self.omega, int(n),
-                  A.ptr(rho_out), A.ptr(u_out), self.flags, A.stream())
+                  A.ptr(rho_out), A.ptr(u_out), self.flags, (self.seed + self.t - 1) & 0xFFFFFFFF,
+                  A.stream())
         if n % 2:
             self.cur = b
         self.t += n
@@ -132,7 +140,7 @@ class Lattice:
                         _lib.call("lbm_lattice_run", self.geo.ref, self.store_id, self.pop[self.cur].data_ptr(),
                                   self.pop[1 - self.cur].data_ptr(), self.pitch, self.aux[self.cur].data_ptr(),
                                   self.aux[1 - self.cur].data_ptr(), self.omega, chunk, 0, 0, self.flags,
-                                  side.cuda_stream)
+                                  (self.seed + self.t - 1) & 0xFFFFFFFF, side.cuda_stream)
                 torch.cuda.current_stream().wait_stream(side)
                 self._graphs[key] = g
             for _ in range(full):

@@ -51,9 +51,9 @@ def test_argument_errors_without_gpu(lib):
         _lib.check(lib.lbm_lattice_read(ctypes.byref(g), 0, None, 32, None, None, None, None, None))
     g.nx = 8
     with pytest.raises(AssertionError, match="omega"):
-        _lib.check(lib.lbm_lattice_run(ctypes.byref(g), 0, 1, 2, 32, None, None, 2.5, 1, None, None, 0, None))
+        _lib.check(lib.lbm_lattice_run(ctypes.byref(g), 0, 1, 2, 32, None, None, 2.5, 1, None, None, 0, 0, None))
     with pytest.raises(AssertionError, match="pitch"):
-        _lib.check(lib.lbm_lattice_run(ctypes.byref(g), 0, 1, 2, 7, None, None, 1.0, 1, None, None, 0, None))
+        _lib.check(lib.lbm_lattice_run(ctypes.byref(g), 0, 1, 2, 7, None, None, 1.0, 1, None, None, 0, 0, None))
 
 
 @pytest.mark.skipif(shutil.which("gcc") is None, reason="gcc not available")

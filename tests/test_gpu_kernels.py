@@ -45,8 +45,8 @@ def test_vectorised_matches_generic(pkg, storage, npt, nx, ny):
         pytest.skip("width not supported by this chunk size")
     f, rho, u = start(nx, ny, nx * 7 + ny)
     for name, bnd in geometries(pkg, nx, ny):
-        a = pkg.Lattice(nx, ny, 1.3, bnd, storage=storage, generic=True).set_state(f, rho, u).step(25)
-        b = pkg.Lattice(nx, ny, 1.3, bnd, storage=storage, npt=npt).set_state(f, rho, u).step(25)
+        a = pkg.Lattice(nx, ny, 1.3, bnd, storage=storage, generic=True, stochastic=False).set_state(f, rho, u).step(25)
+        b = pkg.Lattice(nx, ny, 1.3, bnd, storage=storage, npt=npt, stochastic=False).set_state(f, rho, u).step(25)
         fa, ra, ua = a.read()
         fb, rb, ub = b.read()
         err = float((fa - fb).abs().max() / fa.abs().max())
@@ -63,3 +63,27 @@ def test_vectorised_f64_against_oracle_with_pressure_and_outlet(pkg):
         lat = pkg.Lattice(nx, ny, 1.4, bnd, storage="f64", npt=2).set_state(f, rho, u).step(40)
         got = lat.read()[0].cpu().numpy()
         assert np.abs(got - ref[0]).max() / np.abs(ref[0]).max() <= 1e-12
+
+
+def test_stochastic_rounding_keeps_slow_flows_accurate(pkg):
+    """Couette flow from rest (64x64, moving wall 0.05, 3000 steps): binary16
+    storage with stochastic rounding stays within 1e-3 relative velocity L2 of
+    float64; round-to-nearest loses the small increments near the diffusion front."""
+    n, uw = 64, 0.05
+    m0 = np.zeros((n, n), bool)
+    m0[:, 0] = True
+    m1 = np.zeros((n, n), bool)
+    m1[:, -1] = True
+    B = pkg.boundary_conditions
+    bnd = pkg.boundary_utils.Boundary([B.rigid_wall(m0), B.moving_wall(m1, np.array([uw, 0.0]), 1.0)])
+    rho, u = np.ones((n, n)), np.zeros((n, n, 2))
+    f = O.equilibrium(rho, u)
+    ref = pkg.Lattice(n, n, 1.0, bnd, storage="f64").set_state(f, rho, u).step(3000).moments()[1]
+    errs = {}
+    for st in ("f16", "bf16"):
+        for sr in (True, False):
+            got = pkg.Lattice(n, n, 1.0, bnd, storage=st, stochastic=sr).set_state(f, rho, u).step(3000).moments()[1]
+            errs[(st, sr)] = float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref))
+    assert errs[("f16", True)] <= 1e-3, errs
+    assert errs[("f16", True)] < errs[("f16", False)], errs
+    assert errs[("bf16", True)] < errs[("bf16", False)], errs
