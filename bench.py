@@ -1,6 +1,6 @@
 """Benchmark of the D2Q9 hot path on the sliding-lid cavity (8192^2, omega 1.7,
-lid u = (0.1, 0), rho = 1, u = 0 at start): MLUPS of the resident float64
-fused step, its HBM roofline fraction, the reduced-precision storages, the
+lid u = (0.1, 0), rho = 1, u = 0 at start): MLUPS of the resident fused step
+at float64 accuracy (fx64 storage), its HBM roofline fraction, the reduced-precision storages, the
 end-to-end drop-in call with host buffers, and the NumPy path on host cores.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
@@ -26,7 +26,9 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-BYTES_PER_NODE = {"f64": 144, "f32": 72, "f16": 36, "bf16": 36}
+BYTES_PER_NODE = {"fx64": 144, "f64": 144, "f32": 72, "f16": 36, "bf16": 36}
+# arithmetic of each storage's collision
+DTYPES = {"fx64": "int64+f32x2", "f64": "f64", "f32": "f32", "f16": "f32 (f16 storage)", "bf16": "f32 (bf16 storage)"}
 
 
 def parse():
@@ -36,7 +38,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=8192, help="cavity side")
-    p.add_argument("--storage", default="f64", choices=sorted(BYTES_PER_NODE))
+    p.add_argument("--storage", default="fx64", choices=sorted(BYTES_PER_NODE))
     p.add_argument("--exact", action="store_true", help="NumPy-order float64 arithmetic")
     p.add_argument("--no-extras", action="store_true", help="skip variants, e2e, CPU baseline and the other configs")
     p.add_argument("--workload", default="cavity", choices=["cavity", "shear", "vk", "batch", "serve"],
@@ -60,7 +62,7 @@ def timed_ms(fn):
 
 
 def bench_shear(P):
-    """Shear-wave decay, float64, 64x64 periodic, omega 1.0, 2000 steps: amplitude
+    """Shear-wave decay, fx64 storage, 64x64 periodic, omega 1.0, 2000 steps: amplitude
     decay and the fitted viscosity by the reference's method
     (experiments.py:195-210) against (1/omega - 1/2)/3; also the velocity shear wave."""
     import torch
@@ -91,7 +93,7 @@ def bench_shear(P):
     t = 5 * np.arange(1, 401)
     nu_v = float(curve_fit(lambda t, v: 0.01 * np.exp(-v * k2 * t), t, np.array(vel), p0=[0.1])[0][0])
     theory = (1 / omega - 0.5) / 3
-    return {"workload": "shear wave 64x64, omega 1.0, rho = 1 + 0.01 sin(2 pi x/64), 2000 steps, float64",
+    return {"workload": "shear wave 64x64, omega 1.0, rho = 1 + 0.01 sin(2 pi x/64), 2000 steps, fx64 storage",
             "amplitude_first_last": [float(dens[0]), float(dens[-1])], "nu_theory": theory,
             "nu_fit_density_wave_reference_method": nu_d, "nu_fit_velocity_wave": nu_v,
             "velocity_wave_rel_err": abs(nu_v - theory) / theory, "wall_s_with_per_step_readout": wall}
@@ -110,7 +112,7 @@ def strouhal(trace, L=40, u=0.1, start=None):
 def bench_vk(P, steps=100000):
     """Von Karman precision study: 420x180, plate 40 at x=105 offset +1, inlet
     (0.1, 0) with seeded U(-1e-3, 1e-3) u_y, the reference's outlet,
-    top/bottom bounce-back, Re 100; float64 against float32 / f16 / bf16
+    top/bottom bounce-back, Re 100; float64 storage against fx64 / float32 / f16 / bf16
     storage: velocity L2 error at fixed steps and the Strouhal number from
     the FP64 FFT of u_y at (300, 90)."""
     import torch
@@ -119,7 +121,7 @@ def bench_vk(P, steps=100000):
     f, rho, u, omega, bnd = P.scenarios.von_karman(lx, ly, plate=40, re=100, seed=0)
     checkpoints = [s for s in (10000, 50000, steps) if s <= steps]
     out, ref_u = {}, {}
-    for storage in ("f64", "f32", "f16", "bf16"):
+    for storage in ("f64", "fx64", "f32", "f16", "bf16"):
         m = Member(lx, ly, omega, bnd, steps=steps, probe=(300, 90), f0=f, rho0=rho, u0=u)
         b = Batch([m], storage=storage).start()
         us, ms_total, done = {}, 0.0, 1
@@ -146,7 +148,7 @@ def bench_batch(P, steps=20000, n=256):
     """Batched sweep: 256 von Karman lattices (nx ~ U{200..1200}, ny = nx U(0.3,0.5)
     even, plate ny U(0.1,0.3), Re log-uniform [40, 250], inlet 0.1), f16 storage,
     autotuned tiles, graph-captured; against the same lattices solved one by one
-    in plain float64 (timed on a sample, extrapolated)."""
+    at float64 accuracy (fx64 storage, timed on a sample, extrapolated)."""
     import torch
     from lattice_boltzmann_parallel_solver_gb300.batch import Batch, Member, autotune
     params = P.scenarios.batch_sweep_params(n)
@@ -164,13 +166,13 @@ def bench_batch(P, steps=20000, n=256):
     for m in members:
         m.pop, m.aux = [], []
     torch.cuda.empty_cache()
-    # plain float64 one at a time, each on its own resident lattice, on a sample
+    # float64 accuracy one lattice at a time, each on its own resident lattice, on a sample
     rng = np.random.default_rng(1)
     sample = rng.choice(n, size=12, replace=False)
     t64, nodes64 = 0.0, 0
     for j in sample:
         m = members[j]
-        lat = P.Lattice(m.nx, m.ny, m.omega, m.boundary, storage="f64").set_state(m.f0, m.rho0, m.u0)
+        lat = P.Lattice(m.nx, m.ny, m.omega, m.boundary, storage="fx64").set_state(m.f0, m.rho0, m.u0)
         lat.step(3)
         k = 300
         t64 += timed_ms(lambda: lat.step_graph(k, chunk=100)) / 1e3
@@ -181,8 +183,8 @@ def bench_batch(P, steps=20000, n=256):
     best = min(tune, key=lambda r: r["ms_per_step"])
     return {"workload": "%d von Karman lattices, %d steps each, %.1f M nodes, f16 storage" % (n, steps, nodes / 1e6),
             "aggregate_mlups": agg, "batch_wall_s": ms / 1e3, "autotuned": best,
-            "candidates": len(tune), "f64_sequential_mlups": rate64 / 1e6,
-            "f64_sequential_wall_s_extrapolated": seq_s, "speedup_vs_sequential_f64": seq_s / (ms / 1e3),
+            "candidates": len(tune), "fx64_sequential_mlups": rate64 / 1e6,
+            "fx64_sequential_wall_s_extrapolated": seq_s, "speedup_vs_sequential_fx64": seq_s / (ms / 1e3),
             "omega_range": [min(q["omega"] for q in params), max(q["omega"] for q in params)],
             "stability_risk_instances": sum(q["risky"] for q in params)}
 
@@ -190,12 +192,12 @@ def bench_batch(P, steps=20000, n=256):
 def bench_serve(P, n16=200, n64=40):
     """Serving: seeded Poisson arrivals at 50/s of Couette / Poiseuille / von
     Karman requests with 1k-50k steps, continuous batching under an HBM budget;
-    f16 storage against plain float64; error of f16 results against their solo
-    float64 solve on a sample."""
+    f16 storage against float64 accuracy (fx64 storage); error of f16 results
+    against their solo fx64 solve on a sample."""
     import torch
     from lattice_boltzmann_parallel_solver_gb300.serving import ServingEngine, request_mix, summarize
     out = {}
-    for storage, n in (("f16", n16), ("f64", n64)):
+    for storage, n in (("f16", n16), ("fx64", n64)):
         reqs = request_mix(n, rate=50.0, seed=7)
         eng = ServingEngine(storage=storage, hbm_budget=64 << 30, tick_steps=500)
         done = eng.serve(reqs, realtime=True)
@@ -207,12 +209,12 @@ def bench_serve(P, n16=200, n64=40):
             for r in sorted(done, key=lambda r: r.nodes * r.steps):
                 if budget > 20.0 or len(errs) >= 9:
                     break
-                lat = P.Lattice(r.nx, r.ny, r.omega, r.boundary, storage="f64").set_state(r.f0, r.rho0, r.u0)
+                lat = P.Lattice(r.nx, r.ny, r.omega, r.boundary, storage="fx64").set_state(r.f0, r.rho0, r.u0)
                 t = timed_ms(lambda: lat.step(r.steps)) / 1e3
                 budget += t
                 u64 = lat.moments()[1]
                 errs.setdefault(r.kind, []).append(float(torch.linalg.norm(r.u - u64) / torch.linalg.norm(u64)))
-            out["f16_velocity_l2_rel_err_vs_solo_f64"] = {k: max(v) for k, v in errs.items()}
+            out["f16_velocity_l2_rel_err_vs_solo_fx64"] = {k: max(v) for k, v in errs.items()}
         del done, reqs
         torch.cuda.empty_cache()
     return {"workload": "Poisson 50 req/s mix of Couette / Poiseuille / von Karman, 1k-50k steps, "
@@ -429,7 +431,7 @@ def main():
     if not args.no_extras:
         # reduced-precision storages on the same workload
         variants = {}
-        for st in ("f32", "f16", "bf16"):
+        for st in ("fx64", "f64", "f32", "f16", "bf16"):
             if st == args.storage:
                 continue
             v = make(st)
@@ -479,7 +481,7 @@ def main():
     line = {
         "metric": "MLUPS", "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": per_launch * 1e3, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": args.storage, "data": "synthetic",
+        "vs_baseline": None, "dtype": DTYPES[args.storage], "data": "synthetic",
         "config": {"workload": "sliding-lid cavity %dx%d, omega 1.7, lid u=(0.1,0), rho=1 u=0 start, %s storage%s"
                    % (n, n, args.storage, ", exact arithmetic" if args.exact else ""),
                    "nx": n, "ny": n, "l2": "state %.1f GB, larger than L2" % (2 * BYTES_PER_NODE[args.storage] / 2 * nodes / 1e9),

@@ -73,6 +73,7 @@ typedef struct lbm_geometry {
 #define LBM_STORE_F32 1   /* 36 B per node */
 #define LBM_STORE_F16S 2  /* 18 B per node, f_i - w_i in binary16 */
 #define LBM_STORE_BF16S 3 /* 18 B per node, f_i - w_i in bfloat16 */
+#define LBM_STORE_FX64 4  /* 72 B per node, round(f_i 2^53) in int64: float64 accuracy, no float64 arithmetic */
 
 #define LBM_FLAG_EXACT 1  /* float64 arithmetic in the reference's NumPy operation order, no FMA contraction */
 #define LBM_FLAG_GENERIC 2 /* use the one-node-per-thread kernel instead of the vectorised one */
@@ -163,6 +164,16 @@ int lbm_lattice_run(const lbm_geometry* g, int32_t storage, void* pop_a, void* p
  * (any may be NULL). */
 int lbm_lattice_read(const lbm_geometry* g, int32_t storage, const void* pop, int64_t pitch,
                      const void* aux, double* f_out, double* rho_out, double* u_out, void* stream);
+
+/* ---- exact global moments ---------------------------------------------------------- */
+/* out[3] (device) = (sum rho, sum jx, sum jy) of a reference-layout f[n][9],
+ * summed exactly in 128-bit fixed point (round(f 2^53)), so the result does not
+ * depend on the order of the additions; NaN when some |f| >= 2.  Replaces the
+ * host np.sum checks of the drivers and tests (e.g. tests/test_mass_preservation.py:20-33).
+ * `scratch` holds lbm_reduce_scratch_bytes(n) bytes (device). */
+size_t lbm_reduce_scratch_bytes(int64_t n_nodes);
+int lbm_reduce_moments_f64(const double* f, int64_t n_nodes, void* scratch, size_t scratch_bytes, double* out,
+                           void* stream);
 
 /* ---- batched lattices ----------------------------------------------------------- */
 /* Many lattices of different sizes, one storage type, advanced together: one

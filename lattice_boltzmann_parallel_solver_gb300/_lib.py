@@ -21,7 +21,7 @@ SRC_PULL, SRC_BOUNCE, SRC_CONST, SRC_OUTLET = 0, 1, 2, 3
 KSET_SHIFT, CSET_SHIFT = 18, 22
 MAX_SETS = 16
 
-STORE_F64, STORE_F32, STORE_F16S, STORE_BF16S = 0, 1, 2, 3
+STORE_F64, STORE_F32, STORE_F16S, STORE_BF16S, STORE_FX64 = 0, 1, 2, 3, 4
 FLAG_EXACT = 1
 FLAG_GENERIC = 2
 FLAG_NPT_SHIFT = 4
@@ -77,6 +77,8 @@ SIGNATURES = {
     "lbm_lattice_init": (C.c_int, [GP, i32, vp, vp, vp, f64, vp, i64, vp, i32, vp]),
     "lbm_lattice_run": (C.c_int, [GP, i32, vp, vp, i64, vp, vp, f64, i32, vp, vp, i32, C.c_uint32, vp]),
     "lbm_lattice_read": (C.c_int, [GP, i32, vp, i64, vp, vp, vp, vp, vp]),
+    "lbm_reduce_scratch_bytes": (C.c_size_t, [i64]),
+    "lbm_reduce_moments_f64": (C.c_int, [vp, i64, vp, C.c_size_t, vp, vp]),
     "lbm_batch_table_bytes": (C.c_size_t, [i32]),
     "lbm_batch_build": (C.c_int, [C.POINTER(BatchLattice), i32, i32, i32, vp, C.c_size_t, C.POINTER(i32), vp]),
     "lbm_batch_run": (C.c_int, [vp, i32, i32, i32, i32, i32, vp, i32, i32, vp]),

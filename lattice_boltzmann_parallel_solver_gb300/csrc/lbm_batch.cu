@@ -25,10 +25,15 @@ __global__ void __launch_bounds__(THREADS) batch_kernel(const BatchEntry* __rest
     const int local = tile - __ldg(tile_start + lo);
     const int y = local / e.xblocks, xb = local - y * e.xblocks;
     const bool odd = (g - e.s0) & 1;
-    fused_v2_body<STORE, NPT, true, true>(e.P, odd ? e.pop_b : e.pop_a, odd ? e.pop_a : e.pop_b,
-                                          odd ? e.aux_b : e.aux_a, odd ? e.aux_a : e.aux_b,
-                                          (xb * THREADS + threadIdx.x) * NPT, y,
-                                          hash32(e.P.seed + (uint32_t)(g - e.s0)));
+    const void* pin = odd ? e.pop_b : e.pop_a;
+    void* pout = odd ? e.pop_a : e.pop_b;
+    const void* ain = odd ? e.aux_b : e.aux_a;
+    void* aout = odd ? e.aux_a : e.aux_b;
+    const int x0 = (xb * THREADS + threadIdx.x) * NPT;
+    if constexpr (STORE == LBM_STORE_FX64)
+      fused_fx_body<NPT, true, true>(e.P, pin, pout, ain, aout, x0, y);
+    else
+      fused_v2_body<STORE, NPT, true, true>(e.P, pin, pout, ain, aout, x0, y, hash32(e.P.seed + (uint32_t)(g - e.s0)));
   }
 }
 
@@ -76,6 +81,7 @@ int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_
     e.P.probe_buf = L.probe_buf;
     e.P.probe_count = L.probe_count;
     e.P.seed = L.seed;
+    e.P.qc = fx::q_consts(L.omega);
     e.P.sr = (L.flags & LBM_FLAG_STOCHASTIC) != 0;
     if (L.probe_buf != nullptr && L.probe_count == nullptr)
       return set_error(LBM_ERR_ARG, "a probe needs its counter");
@@ -144,6 +150,8 @@ extern "C" int lbm_batch_run(const void* table, int32_t n, int32_t total_tiles, 
 #define LBM_BATCH_NPT(ST, NP) LBM_BATCH_CASE(ST, NP, 64) LBM_BATCH_CASE(ST, NP, 128) LBM_BATCH_CASE(ST, NP, 256)
   LBM_BATCH_NPT(LBM_STORE_F64, 2)
   LBM_BATCH_NPT(LBM_STORE_F64, 4)
+  LBM_BATCH_NPT(LBM_STORE_FX64, 2)
+  LBM_BATCH_NPT(LBM_STORE_FX64, 4)
   LBM_BATCH_NPT(LBM_STORE_F32, 2)
   LBM_BATCH_NPT(LBM_STORE_F32, 4)
   LBM_BATCH_NPT(LBM_STORE_F16S, 2)

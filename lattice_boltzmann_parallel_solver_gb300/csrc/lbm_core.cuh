@@ -16,6 +16,7 @@
 #include <stdint.h>
 
 #include "../../include/lbm_gb300.h"
+#include "lbm_fx.cuh"
 
 namespace lbm {
 
@@ -42,6 +43,9 @@ template <> struct Store<LBM_STORE_F64> {
   __device__ static void st(T* p, R v, int) { *p = v; }
   __device__ static R to_r(T t, int) { return t; }
   __device__ static T from_r(R v, int) { return v; }
+  using A = R;  // outlet memory: full populations in the working type
+  __device__ static A to_aux(R v, int) { return v; }
+  __device__ static R from_aux(A a, int) { return a; }
   static constexpr bool kShifted = false;
 };
 template <> struct Store<LBM_STORE_F32> {
@@ -51,27 +55,48 @@ template <> struct Store<LBM_STORE_F32> {
   __device__ static void st(T* p, R v, int) { *p = v; }
   __device__ static R to_r(T t, int) { return t; }
   __device__ static T from_r(R v, int) { return v; }
+  using A = R;  // outlet memory: full populations in the working type
+  __device__ static A to_aux(R v, int) { return v; }
+  __device__ static R from_aux(A a, int) { return a; }
   static constexpr bool kShifted = false;
 };
-// shifted storage: the deviation f_i - w_i is kept in 16 bits
+// fixed-point storage: round((f_i - w_i) 2^56) in 64 bits (lbm_fx.cuh); the
+// generic kernels work on its float64 value, the vectorised one on the integers.
+// Its outlet memory keeps the stored integers too (the copy stays exact).
+template <> struct Store<LBM_STORE_FX64> {
+  using T = long long;
+  using R = double;
+  using A = long long;
+  __device__ static R ld(const T* p, int i) { return fx::from_fx(__ldg(p), wd(i)); }
+  __device__ static void st(T* p, R v, int i) { *p = fx::to_fx(v, wd(i)); }
+  __device__ static R to_r(T t, int i) { return fx::from_fx(t, wd(i)); }
+  __device__ static T from_r(R v, int i) { return fx::to_fx(v, wd(i)); }
+  __device__ static A to_aux(R v, int i) { return fx::to_fx(v, wd(i)); }
+  __device__ static R from_aux(A a, int i) { return fx::from_fx(a, wd(i)); }
+  static constexpr bool kShifted = false;
+};
+// shifted storage: the deviation f_i - w_i is kept in 16 bits.  binary16 keeps
+// 1024 (f_i - w_i): deviations down to 6e-8 then stay in the normal range,
+// where stochastic rounding is adding random bits below the kept 10 mantissa
+// bits of the float32 value and truncating.
 template <> struct Store<LBM_STORE_F16S> {
   using T = __half;
   using R = float;
-  __device__ static R ld(const T* p, int i) { return wf(i) + __half2float(__ldg(p)); }
-  __device__ static void st(T* p, R v, int i) { *p = __float2half_rn(v - wf(i)); }
-  __device__ static R to_r(T t, int i) { return wf(i) + __half2float(t); }
-  __device__ static T from_r(R v, int i) { return __float2half_rn(v - wf(i)); }
+  static constexpr float kScale = 1024.0f, kInv = 1.0f / 1024.0f;
+  __device__ static R ld(const T* p, int i) { return fmaf(__half2float(__ldg(p)), kInv, wf(i)); }
+  __device__ static void st(T* p, R v, int i) { *p = __float2half_rn((v - wf(i)) * kScale); }
+  __device__ static R to_r(T t, int i) { return fmaf(__half2float(t), kInv, wf(i)); }
+  __device__ static T from_r(R v, int i) { return __float2half_rn((v - wf(i)) * kScale); }
+  using A = R;  // outlet memory: full populations in the working type
+  __device__ static A to_aux(R v, int) { return v; }
+  __device__ static R from_aux(A a, int) { return a; }
   static constexpr bool kShifted = true;
-  __device__ static R dev(T t) { return __half2float(t); }
-  __device__ static R ld_dev(const T* p) { return __half2float(__ldg(p)); }
-  __device__ static T dev_rn(R d) { return __float2half_rn(d); }
-  // stochastic rounding with 10 random bits: add r/1024 of the binary16 ulp of
-  // |d| (2^(E-10), or 2^-24 below the normal range) away from zero, then truncate
+  __device__ static R dev(T t) { return __half2float(t) * kInv; }
+  __device__ static R ld_dev(const T* p) { return __half2float(__ldg(p)) * kInv; }
+  __device__ static T dev_rn(R d) { return __float2half_rn(d * kScale); }
+  // stochastic rounding with 13 random bits
   __device__ static T dev_sr(R d, uint32_t r) {
-    const uint32_t e = (__float_as_uint(d) >> 23) & 0xFFu;
-    const uint32_t ulp = e >= 113u ? ((e - 10u) << 23) : (103u << 23);
-    const float noise = __uint_as_float(ulp) * ((float)(r & 0x3FFu) * 9.765625e-4f);
-    return __float2half_rz(d + copysignf(noise, d));
+    return __float2half_rz(__uint_as_float(__float_as_uint(d * kScale) + (r & 0x1FFFu)));
   }
 };
 template <> struct Store<LBM_STORE_BF16S> {
@@ -81,6 +106,9 @@ template <> struct Store<LBM_STORE_BF16S> {
   __device__ static void st(T* p, R v, int i) { *p = __float2bfloat16_rn(v - wf(i)); }
   __device__ static R to_r(T t, int i) { return wf(i) + __bfloat162float(t); }
   __device__ static T from_r(R v, int i) { return __float2bfloat16_rn(v - wf(i)); }
+  using A = R;  // outlet memory: full populations in the working type
+  __device__ static A to_aux(R v, int) { return v; }
+  __device__ static R from_aux(A a, int) { return a; }
   static constexpr bool kShifted = true;
   __device__ static R dev(T t) { return __bfloat162float(t); }
   __device__ static R ld_dev(const T* p) { return __bfloat162float(__ldg(p)); }

@@ -2,9 +2,11 @@
 // single-lattice kernels (lbm_lattice.cu) and the batched kernels (lbm_batch.cu).
 #pragma once
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "lbm_core.cuh"
+#include "lbm_fx.cuh"
 #include "lbm_host.h"
 
 namespace lbm {
@@ -52,6 +54,8 @@ struct KParams {
   // seed per step
   uint32_t seed;
   int sr;
+  // fixed-point storage: constants of its collision
+  fx::QConsts qc;
 };
 
 template <typename R>
@@ -197,12 +201,13 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     R g[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) g[i] = f[i][k];
+    const int x = x0 + k;
+    const bool pnode = HAS_PRESSURE && P.g.pressure && k < nvalid && (x == nx - 2 || x == 1);
     const R sum = density9(g);
     const R rho = SH ? R(1) + sum : sum;
     R ux, uy;
     velocity_fast(g, rho, ux, uy);
     if (active && k < nvalid) {
-      const int x = x0 + k;
       if (P.rho_out.p != nullptr) {
         P.rho_out.p[x * P.rho_out.sx + y * P.rho_out.sy] = (double)rho;
         double* up = P.u_out.p + x * P.u_out.sx + y * P.u_out.sy;
@@ -211,18 +216,17 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
       }
       write_probe(P, x, y, ux, uy);
     }
-    if constexpr (SH) collide_dev(g, sum, ux, uy, omega);
-    else collide_fast(g, rho, ux, uy, omega);
-    if (HAS_PRESSURE && P.g.pressure) {
-      const int x = x0 + k;
-      if (k < nvalid && (x == nx - 2 || x == 1)) {
-        R br[9];
-        bracket9_fast(ux, uy, br);
-        const R rb = (R)(x == nx - 2 ? P.g.rho_in : P.g.rho_out) - rho;
+    if constexpr (SH)
+      collide_dev(g, sum, ux, uy, omega);
+    else
+      collide_fast(g, rho, ux, uy, omega);
+    if (pnode) {
+      R br[9];
+      bracket9_fast(ux, uy, br);
+      const R rb = (R)(x == nx - 2 ? P.g.rho_in : P.g.rho_out) - rho;
 #pragma unroll
-        for (int i = 0; i < 9; ++i) pv[i] = fma(wr<R>(i) * br[i], rb, g[i]);
-        pcol = x;
-      }
+      for (int i = 0; i < 9; ++i) pv[i] = fma(wr<R>(i) * br[i], rb, g[i]);
+      pcol = x;
     }
 #pragma unroll
     for (int i = 0; i < 9; ++i) f[i][k] = g[i];
@@ -235,19 +239,11 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     if constexpr (SH) return sr ? St::dev_sr(v, rbits) : St::dev_rn(v);
     else return St::from_r(v, i);
   };
-  uint32_t hk[NPT][3];
+  // random bits: one hash per node, then one multiply-add step per direction;
+  // each store takes 16 high bits
+  uint32_t hk[NPT];
 #pragma unroll
-  for (int k = 0; k < NPT; ++k) {
-    if (sr) {
-      const uint32_t h0 = hash32((uint32_t)(y * nx + x0 + k) * 0x9E3779B1u ^ seed);
-      hk[k][0] = h0;
-      hk[k][1] = hash32(h0 + 0x68E31DA4u);
-      hk[k][2] = hash32(h0 + 0xB5297A4Du);
-    } else {
-      hk[k][0] = hk[k][1] = hk[k][2] = 0u;
-    }
-  }
-#define LBM_RBITS(k, i) (hk[k][(i) / 3] >> (10 * ((i) % 3)))
+  for (int k = 0; k < NPT; ++k) hk[k] = sr ? hash32((uint32_t)(y * nx + x0 + k) * 0x9E3779B1u ^ seed) : 0u;
   T* pout = static_cast<T*>(pop_out_v);
   const bool pr = HAS_PRESSURE && P.g.pressure;
   if (nvalid == NPT && !(pr && (first || last))) {
@@ -255,7 +251,10 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     for (int i = 0; i < 9; ++i) {
       T raw[NPT];
 #pragma unroll
-      for (int k = 0; k < NPT; ++k) raw[k] = to_store(f[i][k], i, LBM_RBITS(k, i));
+      for (int k = 0; k < NPT; ++k) {
+        raw[k] = to_store(f[i][k], i, hk[k] >> 16);
+        hk[k] = hk[k] * 0x2C1B3C6Du + 0x297A2D39u;
+      }
       st_vec<T, NPT>(pout + i * plane + r0 + x0, raw);
     }
   } else {
@@ -268,19 +267,199 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
         const int x = x0 + k;
         const bool skip = k >= nvalid || (pr && ((x == 0 && ((P.g.pin >> i) & 1u)) ||
                                                  (x == nx - 1 && ((P.g.pout >> i) & 1u))));
-        if (!skip) pout[i * plane + r0 + x] = to_store(f[i][k], i, LBM_RBITS(k, i));
+        if (!skip) pout[i * plane + r0 + x] = to_store(f[i][k], i, hk[k] >> 16);
+        hk[k] = hk[k] * 0x2C1B3C6Du + 0x297A2D39u;
       }
     }
   }
   if (pr && pcol >= 0) {
     const uint32_t dirs = pcol == nx - 2 ? P.g.pin : P.g.pout;
     const int dst = pcol == nx - 2 ? 0 : nx - 1;
-    const uint32_t hp = sr ? hash32((uint32_t)(y * nx + dst) * 0x9E3779B1u ^ seed ^ 0x5bd1e995u) : 0u;
+    uint32_t hp = sr ? hash32((uint32_t)(y * nx + dst) * 0x9E3779B1u ^ seed ^ 0x5bd1e995u) : 0u;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+      if ((dirs >> i) & 1u) pout[i * plane + r0 + dst] = to_store(pv[i], i, hp >> 16);
+      hp = hp * 0x2C1B3C6Du + 0x297A2D39u;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Vectorised fused step of the fixed-point storage (LBM_STORE_FX64).  The same
+// chunking, shuffles and boundary sources as fused_v2_body, on 64-bit integers:
+// pull, bounce-back and the outlet copy move populations exactly, the boundary
+// constants are rounded to fixed point, and fx::collide_q collides each node in
+// its range.  Nodes outside it, the moments written out (last step, probe) and
+// the pressure rewrite of columns 0 / nx-1 use float64 on the converted values.
+// The outlet memory holds the stored integers, as in the generic kernel.
+// ---------------------------------------------------------------------------
+template <int NPT, bool HAS_BC, bool HAS_PRESSURE>
+__device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_in_v, void* pop_out_v,
+                                              const void* aux_in_v, void* aux_out_v, int x0, int y) {
+  using T = long long;
+  const int lane = threadIdx.x & 31;
+  const int nx = P.g.nx, ny = P.g.ny;
+  const int xlast = ((nx - 1) / NPT) * NPT;
+  const bool active = x0 < nx;
+  if (!active) x0 = xlast;
+  const int nvalid = min(NPT, nx - x0);
+  const int pitch = (int)P.pitch, plane = (int)P.plane;
+  const int ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
+  const int r0 = y * pitch, rm = ym * pitch, rp = yp * pitch;
+  const bool first = x0 == 0;
+  const bool last = x0 == xlast;
+  const int xm = first ? nx - 1 : x0 - 1;
+  const int xp = x0 + NPT >= nx ? 0 : x0 + NPT;
+  const T* pin = static_cast<const T*>(pop_in_v);
+
+  T f[9][NPT];
+#pragma unroll
+  for (int i = 0; i < 9; ++i) {
+    const int row = cy(i) == 1 ? rm : (cy(i) == -1 ? rp : r0);
+    const T* base = pin + i * plane + row;
+    T v[NPT];
+    ld_vec<T, NPT>(base + x0, v);
+    if (cx(i) == 0) {
+#pragma unroll
+      for (int k = 0; k < NPT; ++k) f[i][k] = v[k];
+    } else if (cx(i) == 1) {
+      T prev = __shfl_up_sync(0xffffffffu, v[NPT - 1], 1);
+      if (lane == 0 || first) prev = __ldg(base + xm);
+      f[i][0] = prev;
+#pragma unroll
+      for (int k = 1; k < NPT; ++k) f[i][k] = v[k - 1];
+    } else {
+      T next = __shfl_down_sync(0xffffffffu, v[0], 1);
+      if (lane == 31 || last) next = __ldg(base + xp);
+#pragma unroll
+      for (int k = 0; k < NPT - 1; ++k) f[i][k] = v[k + 1];
+      f[i][NPT - 1] = next;
+      if (nvalid < NPT) {
+#pragma unroll
+        for (int k = 0; k < NPT; ++k) {
+          const int xs = x0 + k + 1 < nx ? x0 + k + 1 : 0;
+          f[i][k] = __ldg(base + xs);
+        }
+      }
+    }
+  }
+
+  if (HAS_BC && P.g.bcmask != nullptr) {
+    const uint32_t word = __ldg(P.g.bcmask + y * P.g.words + (x0 >> 5));
+    const uint32_t bits = (word >> (x0 & 31)) & ((NPT >= 32) ? 0xffffffffu : ((1u << NPT) - 1u));
+    if (bits) {
+      const T* aux_in = static_cast<const T*>(aux_in_v);
+#pragma unroll
+      for (int k = 0; k < NPT; ++k) {
+        if (!((bits >> k) & 1u)) continue;
+        const int x = x0 + k;
+        const uint32_t d = __ldg(P.g.desc + y * nx + x);
+        const int ks = (d >> LBM_DESC_KSET_SHIFT) & 15, cs = (d >> LBM_DESC_CSET_SHIFT) & 15;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+          const uint32_t s = (d >> (2 * i)) & 3u;
+          if (s == LBM_SRC_BOUNCE)
+            f[i][k] = __ldg(pin + opp(i) * plane + r0 + x) - fx::round_scaled(P.g.kconst[ks][i], fx::kS);
+          else if (s == LBM_SRC_CONST)
+            f[i][k] = fx::to_fx(P.g.cconst[cs][i], wd(i));
+          else if (s == LBM_SRC_OUTLET && outlet_slot(i) >= 0 && aux_in != nullptr)
+            f[i][k] = aux_in[outlet_slot(i) * ny + y];
+        }
+      }
+    }
+  }
+
+  if (aux_out_v != nullptr && active && x0 <= nx - 2 && nx - 2 < x0 + NPT) {
+    T* aux_out = static_cast<T*>(aux_out_v);
+    const int ka = nx - 2 - x0;
+    T a3 = f[3][0], a6 = f[6][0], a7 = f[7][0];
+#pragma unroll
+    for (int k = 1; k < NPT; ++k) {
+      a3 = k == ka ? f[3][k] : a3;
+      a6 = k == ka ? f[6][k] : a6;
+      a7 = k == ka ? f[7][k] : a7;
+    }
+    aux_out[0 * ny + y] = a3;
+    aux_out[1 * ny + y] = a6;
+    aux_out[2 * ny + y] = a7;
+  }
+
+  T pv[9];  // pressure rewrite computed by the node at column nx-2 or 1
+  int pcol = -1;
+#pragma unroll
+  for (int k = 0; k < NPT; ++k) {
+    int64_t g[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) g[i] = f[i][k];
+    const int x = x0 + k;
+    const bool pnode = HAS_PRESSURE && P.g.pressure && k < nvalid && (x == nx - 2 || x == 1);
+    const bool out = active && k < nvalid &&
+                     (P.rho_out.p != nullptr || (P.probe_buf != nullptr && x == P.probe_x && y == P.probe_y));
+    double rho = 1.0, ux = 0.0, uy = 0.0;
+    if (out || pnode) {
+      double d[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) d[i] = fx::from_fx(g[i], wd(i));
+      rho = density9(d);
+      velocity_fast(d, rho, ux, uy);
+      if (out) {
+        if (P.rho_out.p != nullptr) {
+          P.rho_out.p[x * P.rho_out.sx + y * P.rho_out.sy] = rho;
+          double* up = P.u_out.p + x * P.u_out.sx + y * P.u_out.sy;
+          up[0] = ux;
+          up[P.u_out.sc] = uy;
+        }
+        write_probe(P, x, y, ux, uy);
+      }
+    }
+    if (!fx::collide_q(g, P.qc)) {
+      double d[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) d[i] = fx::from_fx(g[i], wd(i));
+      const double r2 = density9(d);
+      double u2x, u2y;
+      velocity_fast(d, r2, u2x, u2y);
+      collide_fast(d, r2, u2x, u2y, P.omega);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) g[i] = fx::to_fx(d[i], wd(i));
+    }
+    if (pnode) {
+      double br[9];
+      bracket9_fast(ux, uy, br);
+      const double rb = (x == nx - 2 ? P.g.rho_in : P.g.rho_out) - rho;
+#pragma unroll
+      for (int i = 0; i < 9; ++i) pv[i] = fx::to_fx(fma(wd(i) * br[i], rb, fx::from_fx(g[i], wd(i))), wd(i));
+      pcol = x;
+    }
+#pragma unroll
+    for (int i = 0; i < 9; ++i) f[i][k] = g[i];
+  }
+
+  if (!active) return;
+  T* pout = static_cast<T*>(pop_out_v);
+  const bool pr = HAS_PRESSURE && P.g.pressure;
+  if (nvalid == NPT && !(pr && (first || last))) {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) st_vec<T, NPT>(pout + i * plane + r0 + x0, f[i]);
+  } else {
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+#pragma unroll
+      for (int k = 0; k < NPT; ++k) {
+        const int x = x0 + k;
+        const bool skip = k >= nvalid || (pr && ((x == 0 && ((P.g.pin >> i) & 1u)) ||
+                                                 (x == nx - 1 && ((P.g.pout >> i) & 1u))));
+        if (!skip) pout[i * plane + r0 + x] = f[i][k];
+      }
+    }
+  }
+  if (pr && pcol >= 0) {
+    const uint32_t dirs = pcol == nx - 2 ? P.g.pin : P.g.pout;
+    const int dst = pcol == nx - 2 ? 0 : nx - 1;
 #pragma unroll
     for (int i = 0; i < 9; ++i)
-      if ((dirs >> i) & 1u) pout[i * plane + r0 + dst] = to_store(pv[i], i, hp >> (3 * i));
+      if ((dirs >> i) & 1u) pout[i * plane + r0 + dst] = pv[i];
   }
-#undef LBM_RBITS
 }
 
 // ---------------------------------------------------------------------------

@@ -32,7 +32,8 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
   const int nx = P.g.nx, ny = P.g.ny;
   if (x >= nx || y >= ny) return;
   const int64_t r0 = (int64_t)y * P.pitch;
-  const R* aux_in = static_cast<const R*>(P.aux_in);
+  using A = typename St::A;
+  const A* aux_in = static_cast<const A*>(P.aux_in);
 
   R f[9];
   if (MODE == MODE_INIT) {
@@ -68,7 +69,7 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
           } else if (s == LBM_SRC_CONST) {
             f[i] = (R)P.g.cconst[cs][i];
           } else if (s == LBM_SRC_OUTLET && outlet_slot(i) >= 0 && aux_in != nullptr) {
-            f[i] = aux_in[outlet_slot(i) * ny + y];
+            f[i] = St::from_aux(aux_in[outlet_slot(i) * ny + y], i);
           }
         }
       }
@@ -77,10 +78,10 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
 
   // outlet memory: the pre-collision populations 3,6,7 of column nx-2
   if (MODE != MODE_READ && P.aux_out != nullptr && x == nx - 2) {
-    R* aux_out = static_cast<R*>(P.aux_out);
-    aux_out[0 * ny + y] = f[3];
-    aux_out[1 * ny + y] = f[6];
-    aux_out[2 * ny + y] = f[7];
+    A* aux_out = static_cast<A*>(P.aux_out);
+    aux_out[0 * ny + y] = St::to_aux(f[3], 3);
+    aux_out[1 * ny + y] = St::to_aux(f[6], 6);
+    aux_out[2 * ny + y] = St::to_aux(f[7], 7);
   }
 
   // moments of f_n; the collision of the first step uses the rho,u passed in
@@ -183,6 +184,12 @@ __global__ void __launch_bounds__(THREADS) fused_v2_kernel(const __grid_constant
                                                   (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y, P.seed);
 }
 
+template <int NPT, int THREADS, bool HAS_BC, bool HAS_PRESSURE>
+__global__ void __launch_bounds__(THREADS) fused_fx_kernel(const __grid_constant__ KParams P) {
+  fused_fx_body<NPT, HAS_BC, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out,
+                                           (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y);
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -212,32 +219,53 @@ static int dispatch(int storage, bool exact, const KParams& P, cudaStream_t s) {
     case LBM_STORE_F32: return launch<LBM_STORE_F32, false, MODE>(P, s);
     case LBM_STORE_F16S: return launch<LBM_STORE_F16S, false, MODE>(P, s);
     case LBM_STORE_BF16S: return launch<LBM_STORE_BF16S, false, MODE>(P, s);
+    case LBM_STORE_FX64: return launch<LBM_STORE_FX64, false, MODE>(P, s);
     default: return set_error(LBM_ERR_ARG, "unknown storage type");
   }
 }
 
 constexpr int kV2Threads = 128;
 
+// the four boundary specialisations of one vectorised kernel
+#define LBM_LAUNCH_SPECIALISED(KERNEL, ...)                                            \
+  do {                                                                                 \
+    const bool bc = P.g.bcmask != nullptr, pr = P.g.pressure != 0;                     \
+    if (bc && pr)                                                                      \
+      KERNEL<__VA_ARGS__, true, true><<<grid, kV2Threads, 0, s>>>(P);                  \
+    else if (bc)                                                                       \
+      KERNEL<__VA_ARGS__, true, false><<<grid, kV2Threads, 0, s>>>(P);                 \
+    else if (pr)                                                                       \
+      KERNEL<__VA_ARGS__, false, true><<<grid, kV2Threads, 0, s>>>(P);                 \
+    else                                                                               \
+      KERNEL<__VA_ARGS__, false, false><<<grid, kV2Threads, 0, s>>>(P);                \
+  } while (0)
+
+template <int NPT>
+static dim3 v2_grid(const KParams& P) {
+  const int chunks = (P.g.nx + NPT - 1) / NPT;
+  return dim3((unsigned)((chunks + kV2Threads - 1) / kV2Threads), (unsigned)P.g.ny, 1);
+}
+
 template <int STORE, int NPT>
 static int launch_v2(const KParams& P, cudaStream_t s) {
-  const int chunks = (P.g.nx + NPT - 1) / NPT;
-  const dim3 grid((unsigned)((chunks + kV2Threads - 1) / kV2Threads), (unsigned)P.g.ny, 1);
-  const bool bc = P.g.bcmask != nullptr, pr = P.g.pressure != 0;
-  if (bc && pr)
-    fused_v2_kernel<STORE, NPT, kV2Threads, true, true><<<grid, kV2Threads, 0, s>>>(P);
-  else if (bc)
-    fused_v2_kernel<STORE, NPT, kV2Threads, true, false><<<grid, kV2Threads, 0, s>>>(P);
-  else if (pr)
-    fused_v2_kernel<STORE, NPT, kV2Threads, false, true><<<grid, kV2Threads, 0, s>>>(P);
-  else
-    fused_v2_kernel<STORE, NPT, kV2Threads, false, false><<<grid, kV2Threads, 0, s>>>(P);
+  const dim3 grid = v2_grid<NPT>(P);
+  LBM_LAUNCH_SPECIALISED(fused_v2_kernel, STORE, NPT, kV2Threads);
   count_launch();
   return check_launch("fused_v2_kernel");
 }
 
+template <int NPT>
+static int launch_fx(const KParams& P, cudaStream_t s) {
+  const dim3 grid = v2_grid<NPT>(P);
+  LBM_LAUNCH_SPECIALISED(fused_fx_kernel, NPT, kV2Threads);
+  count_launch();
+  return check_launch("fused_fx_kernel");
+}
+
 static int default_npt(int storage) {
   switch (storage) {
-    case LBM_STORE_F64: return 2;
+    case LBM_STORE_F64:
+    case LBM_STORE_FX64: return 2;
     case LBM_STORE_F32: return 4;
     default: return 4;
   }
@@ -257,6 +285,8 @@ static int launch_fused(int storage, int flags, const KParams& P, cudaStream_t s
   switch (storage * 16 + npt) {
     case LBM_STORE_F64 * 16 + 2: return launch_v2<LBM_STORE_F64, 2>(P, s);
     case LBM_STORE_F64 * 16 + 4: return launch_v2<LBM_STORE_F64, 4>(P, s);
+    case LBM_STORE_FX64 * 16 + 2: return launch_fx<2>(P, s);
+    case LBM_STORE_FX64 * 16 + 4: return launch_fx<4>(P, s);
     case LBM_STORE_F32 * 16 + 2: return launch_v2<LBM_STORE_F32, 2>(P, s);
     case LBM_STORE_F32 * 16 + 4: return launch_v2<LBM_STORE_F32, 4>(P, s);
     case LBM_STORE_F16S * 16 + 2: return launch_v2<LBM_STORE_F16S, 2>(P, s);
@@ -271,7 +301,8 @@ static int launch_fused(int storage, int flags, const KParams& P, cudaStream_t s
 
 static size_t store_bytes(int storage) {
   switch (storage) {
-    case LBM_STORE_F64: return 8;
+    case LBM_STORE_F64:
+    case LBM_STORE_FX64: return 8;
     case LBM_STORE_F32: return 4;
     case LBM_STORE_F16S:
     case LBM_STORE_BF16S: return 2;
@@ -338,6 +369,7 @@ int lbm_lattice_run(const lbm_geometry* g, int32_t storage, void* pop_a, void* p
   P.plane = pitch * g->ny;
   P.omega = omega;
   P.sr = (flags & LBM_FLAG_STOCHASTIC) != 0;
+  P.qc = fx::q_consts(omega);
   for (int s = 0; s < nsteps; ++s) {
     P.seed = hash32(seed + (uint32_t)s);
     const bool even = (s % 2) == 0;

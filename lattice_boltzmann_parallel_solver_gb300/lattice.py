@@ -3,9 +3,12 @@
 
 The populations live on the device as structure-of-arrays planes
 pop[9][ny][pitch] (x contiguous, pitch a multiple of 32 elements) in one of
-four storage forms:
+five storage forms:
 
-  "f64"   float64 storage and arithmetic: the drop-in (72 B per node)
+  "fx64"  round((f_i - w_i) 2^56) in int64, exact integer moments and
+          linear relaxation, float-float quadratic term: float64 accuracy
+          without float64 instructions (72 B per node; the default)
+  "f64"   float64 storage and arithmetic, the drop-in's form (72 B)
   "f32"   float32 storage and arithmetic (36 B)
   "f16"   float32 arithmetic, f_i - w_i stored in binary16 (18 B)
   "bf16"  float32 arithmetic, f_i - w_i stored in bfloat16 (18 B)
@@ -16,6 +19,7 @@ moments, collides and writes the new post-collision populations once.
 """
 from __future__ import annotations
 
+import numpy as np
 import torch
 
 from . import _arrays as A
@@ -23,27 +27,32 @@ from . import _lib
 from .geometry import empty_geometry
 
 STORAGES = {
+    "fx64": (_lib.STORE_FX64, torch.int64, torch.int64),
     "f64": (_lib.STORE_F64, torch.float64, torch.float64),
     "f32": (_lib.STORE_F32, torch.float32, torch.float32),
     "f16": (_lib.STORE_F16S, torch.float16, torch.float32),
     "bf16": (_lib.STORE_BF16S, torch.bfloat16, torch.float32),
 }
-BYTES_PER_NODE = {"f64": 144, "f32": 72, "f16": 36, "bf16": 36}
+BYTES_PER_NODE = {"fx64": 144, "f64": 144, "f32": 72, "f16": 36, "bf16": 36}
 
 
 class Lattice:
     """An nx x ny D2Q9 lattice with a fused boundary composition, resident on the device."""
 
-    def __init__(self, nx: int, ny: int, omega: float, boundary=None, storage: str = "f64",
+    def __init__(self, nx: int, ny: int, omega: float, boundary=None, storage: str = None,
                  exact: bool = False, device: str = "cuda", generic: bool = False, npt: int = 0,
                  stochastic: bool = None, seed: int = 0):
         """``generic`` forces the one-node-per-thread kernel; ``npt`` sets the
         nodes per thread of the vectorised kernel (0 = the default for the storage).
         ``stochastic`` (default: on for the 16-bit storages) rounds the stored
         deviations stochastically, which keeps increments smaller than half a
-        16-bit step from being lost; ``seed`` seeds its random bits."""
+        16-bit step from being lost; ``seed`` seeds its random bits.  The
+        default storage is "fx64", or "f64" with ``exact`` (the reference's
+        float64 operation order, bit for bit)."""
         A.require_cuda()
         assert 0 < omega < 2
+        if storage is None:
+            storage = "f64" if exact else "fx64"
         assert storage in STORAGES, "storage must be one of %s" % sorted(STORAGES)
         assert not (exact and storage != "f64"), "exact arithmetic needs float64 storage"
         self.nx, self.ny, self.omega = int(nx), int(ny), float(omega)
@@ -169,3 +178,50 @@ class Lattice:
     def moments(self):
         _, rho, u = self.read(want_f=False)
         return rho, u
+
+    # -- checkpoint / resume -----------------------------------------------------
+    def checkpoint(self) -> dict:
+        """The resident state (populations, outlet memory, step count) as host
+        arrays; ``restore`` continues bit for bit from it."""
+        if self._init is not None:
+            f, rho, u = self._init
+            return {"pending": np.asarray(1), "f": f.cpu().numpy(),
+                    "rho": None if rho is None else rho.cpu().numpy(),
+                    "u": None if u is None else u.cpu().numpy(), "t": np.asarray(self.t)}
+        pop = self.pop[self.cur]
+        pop = pop.view(torch.int16).cpu().numpy().view(np.uint16) if self.pop_dtype == torch.bfloat16 \
+            else pop.cpu().numpy()
+        return {"pending": np.asarray(0), "pop": pop,
+                "aux": self.aux[self.cur].cpu().numpy(), "t": np.asarray(self.t),
+                "storage": np.asarray(self.storage), "nx": np.asarray(self.nx), "ny": np.asarray(self.ny)}
+
+    def restore(self, ck: dict):
+        if int(ck["pending"]):
+            self.set_state(ck["f"], ck.get("rho"), ck.get("u"))
+            self.t = int(ck["t"])
+            return self
+        assert str(ck["storage"]) == self.storage and int(ck["nx"]) == self.nx and int(ck["ny"]) == self.ny
+        self._init = None
+        self.cur = 0
+        pop = np.asarray(ck["pop"])
+        src = torch.from_numpy(pop.view(np.int16)).view(torch.bfloat16) if pop.dtype == np.uint16 \
+            else torch.from_numpy(pop)
+        self.pop[0].copy_(src)
+        self.aux[0].copy_(torch.from_numpy(np.asarray(ck["aux"])))
+        self.t = int(ck["t"])
+        self._graphs.clear()
+        return self
+
+    def save(self, path: str):
+        """Write a checkpoint file (.npz)."""
+        ck = self.checkpoint()
+        np.savez(path, **{k: v for k, v in ck.items() if v is not None})
+
+    def load(self, path: str):
+        with np.load(path, allow_pickle=False) as z:
+            ck = {k: z[k] for k in z.files}
+        ck.setdefault("rho", None)
+        ck.setdefault("u", None)
+        if "pop" in ck and self.pop_dtype == torch.bfloat16:
+            ck["pop"] = ck["pop"].view(np.uint16)
+        return self.restore(ck)

@@ -110,7 +110,7 @@ class ServingEngine:
         self.stats = {"ticks": 0, "max_live": 0, "steps": 0}
 
     def state_bytes(self, req):
-        per = {"f64": 8, "f32": 4, "f16": 2, "bf16": 2}[self.storage]
+        per = {"fx64": 8, "f64": 8, "f32": 4, "f16": 2, "bf16": 2}[self.storage]
         pitch = (req.nx + 31) // 32 * 32
         return 2 * 9 * req.ny * pitch * per + 2 * 3 * req.ny * 8
 

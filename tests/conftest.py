@@ -16,3 +16,11 @@ def pytest_configure(config):
 def golden():
     import numpy as np
     return dict(np.load(os.path.join(ROOT, "tests", "golden", "reference_fixtures.npz")))
+
+
+@pytest.fixture(scope="session")
+def extended():
+    """Extended-precision (80-bit) runs of periodic cases, made by
+    tests/golden/make_extended.py."""
+    import numpy as np
+    return dict(np.load(os.path.join(ROOT, "tests", "golden", "extended_precision.npz")))

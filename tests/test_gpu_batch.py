@@ -42,7 +42,7 @@ def alone(pkg, m, storage, npt):
     return lat.set_state(m.f0, m.rho0, m.u0).step(m.steps)
 
 
-@pytest.mark.parametrize("storage,npt,threads", [("f64", 2, 128), ("f32", 4, 64), ("f16", 4, 128),
+@pytest.mark.parametrize("storage,npt,threads", [("fx64", 2, 128), ("fx64", 4, 64), ("f64", 2, 128), ("f32", 4, 64), ("f16", 4, 128),
                                                  ("f16", 8, 256), ("bf16", 2, 128)])
 def test_batch_members_equal_lone_runs(pkg, storage, npt, threads):
     from lattice_boltzmann_parallel_solver_gb300.batch import Batch
@@ -53,13 +53,14 @@ def test_batch_members_equal_lone_runs(pkg, storage, npt, threads):
         got = b.read(j)[0]
         ref = alone(pkg, m, storage, npt).read()[0]
         err = float((got - ref).abs().max() / ref.abs().max())
-        assert err <= (1e-13 if storage == "f64" else 1e-6), (j, err)
+        assert err <= (1e-13 if storage in ("f64", "fx64") else 1e-6), (j, err)
 
 
-def test_batch_f64_against_oracle(pkg):
+@pytest.mark.parametrize("storage", ["fx64", "f64"])
+def test_batch_f64_against_oracle(pkg, storage):
     from lattice_boltzmann_parallel_solver_gb300.batch import Batch
     ms = members(pkg)
-    b = Batch(ms, storage="f64").start()
+    b = Batch(ms, storage=storage).start()
     b.run()
     cav = ms[2]
     ref = O.run(cav.f0, cav.rho0, cav.u0, 1.7, cav.steps, O.cavity_boundary(37, 37, 0.1, 1.0))

@@ -67,17 +67,19 @@ def test_resident_f64_exact_and_fast(pkg, name, steps):
     got = [t.cpu().numpy() for t in lat.read()]
     for a, b in zip(got, ref):
         assert np.array_equal(a, b)
-    lat = pkg.Lattice(nx, ny, om, pbnd(), storage="f64").set_state(f, rho, u).step(steps)
-    got = [t.cpu().numpy() for t in lat.read()]
-    assert rel(got[0], ref[0]) <= TOL
-    assert rel(got[1], ref[1]) <= TOL
+    for storage in ("f64", "fx64"):
+        lat = pkg.Lattice(nx, ny, om, pbnd(), storage=storage).set_state(f, rho, u).step(steps)
+        got = [t.cpu().numpy() for t in lat.read()]
+        assert rel(got[0], ref[0]) <= TOL, storage
+        assert rel(got[1], ref[1]) <= TOL, storage
 
 
+@pytest.mark.parametrize("storage", ["f64", "fx64"])
 @pytest.mark.parametrize("name", ["shear", "couette", "cavity"])
-def test_resident_f64_2000_steps(pkg, name):
+def test_resident_f64_2000_steps(pkg, name, storage):
     nx, ny, om, f, rho, u, obnd, pbnd = scenario(name)
     ref = O.run(f, rho, u, om, 2000, obnd)
-    lat = pkg.Lattice(nx, ny, om, pbnd(), storage="f64").set_state(f, rho, u).step(2000)
+    lat = pkg.Lattice(nx, ny, om, pbnd(), storage=storage).set_state(f, rho, u).step(2000)
     assert rel(lat.read()[0].cpu().numpy(), ref[0]) <= TOL
 
 
@@ -157,17 +159,41 @@ def test_shear_wave_viscosity_law(pkg):
         assert abs(nu - (1 / om - 0.5) / 3) / ((1 / om - 0.5) / 3) < 0.01
 
 
-def test_density_wave_fit_matches_oracle(pkg):
-    """Config 1 (rho = 1 + 0.01 sin(2 pi x/64), omega 1, 2000 steps): the per-step
-    amplitude trace agrees with the oracle's."""
+@pytest.mark.parametrize("storage", ["f64", "fx64"])
+def test_density_wave_fit_matches_oracle(pkg, extended, storage):
+    """Density wave rho = 1 + 0.01 sin(2 pi x / 64) on 64 x 64, omega 1, 2000
+    steps: the amplitude trace (every 100 steps) agrees with the oracle's.
+    The float64 storage shares NumPy's rounding pattern and stays within 1e-13
+    of it; the fixed-point storage is within 1e-15 of the extended-precision
+    run, while NumPy's own float64 trace drifts from that by about 1e-13, so
+    against the oracle it is held to the 1e-12 float64 gate."""
     nx, ny, om, f, rho, u, _, _ = scenario("shear")
-    lat = pkg.Lattice(nx, ny, om).set_state(f, rho, u)
-    fo, ro, uo = f, rho, u
-    for _ in range(20):
+    lat = pkg.Lattice(nx, ny, om, storage=storage).set_state(f)
+    fo, ro, uo = f, O.density(f), O.velocity(O.density(f), f)
+    amp = extended["density_wave_amp"]
+    for k in range(20):
         lat.step(100)
         fo, ro, uo = O.run(fo, ro, uo, om, 100)
         r = lat.moments()[0].cpu().numpy()
-        assert abs(np.abs(r - 1).max() - np.abs(ro - 1).max()) <= 1e-13
+        a = np.abs(r - 1).max()
+        if storage == "f64":
+            assert abs(a - np.abs(ro - 1).max()) <= 1e-13
+        else:
+            assert abs(a - np.abs(ro - 1).max()) <= 1e-12
+            assert abs(a - amp[k]) <= 1e-15, (k, a - amp[k])
+    if storage == "fx64":
+        assert np.abs(r[:, 0] - extended["density_wave_rho_x"]).max() <= 1e-15
+
+
+def test_fixed_point_tracks_extended_precision(pkg, extended):
+    """Random periodic state (32 x 24, omega 1.3, 500 steps): the fixed-point
+    storage stays within 1e-15 of the extended-precision solution."""
+    rng = np.random.default_rng(0)
+    rho = rng.uniform(0.95, 1.05, (32, 24))
+    u = rng.normal(0, 0.05, (32, 24, 2))
+    f = O.equilibrium(rho, u)
+    got = pkg.Lattice(32, 24, 1.3, storage="fx64").set_state(f).step(500).read()[0].cpu().numpy()
+    assert np.abs(got - extended["random_f"]).max() <= 1e-15
 
 
 @pytest.mark.parametrize("storage,tol", [("f32", 1e-4), ("f16", 1e-3), ("bf16", 1e-2)])

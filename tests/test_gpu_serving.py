@@ -47,7 +47,7 @@ def clone(r, rid, arrival):
     return Request(rid, r.kind, r.nx, r.ny, r.omega, r.steps, r.boundary, r.f0, r.rho0, r.u0, arrival, dict(r.params))
 
 
-@pytest.mark.parametrize("storage", ["f16", "f64"])
+@pytest.mark.parametrize("storage", ["f16", "fx64"])
 def test_same_result_alone_and_in_mix(pkg, storage):
     from lattice_boltzmann_parallel_solver_gb300.serving import ServingEngine
     reqs = small_mix(pkg)
