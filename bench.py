@@ -34,7 +34,7 @@ DTYPES = {"fx64": "int64+f32x2", "f64": "f64", "f32": "f32", "f16": "f32 (f16 st
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=500)
+    p.add_argument("--steps", type=int, default=5000)
     p.add_argument("--warmup", type=int, default=20)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--n", type=int, default=8192, help="cavity side")
@@ -166,25 +166,28 @@ def bench_batch(P, steps=20000, n=256):
     for m in members:
         m.pop, m.aux = [], []
     torch.cuda.empty_cache()
-    # float64 accuracy one lattice at a time, each on its own resident lattice, on a sample
+    # the same lattices one at a time, each on its own resident lattice, on a
+    # sample: plain float64 (the drop-in's storage and FMA collision) and fx64
     rng = np.random.default_rng(1)
     sample = rng.choice(n, size=12, replace=False)
-    t64, nodes64 = 0.0, 0
-    for j in sample:
-        m = members[j]
-        lat = P.Lattice(m.nx, m.ny, m.omega, m.boundary, storage="fx64").set_state(m.f0, m.rho0, m.u0)
-        lat.step(3)
-        k = 300
-        t64 += timed_ms(lambda: lat.step_graph(k, chunk=100)) / 1e3
-        nodes64 += m.nodes * k
-        del lat
-    rate64 = nodes64 / t64
-    seq_s = nodes * steps / rate64
+    seq = {}
+    for storage in ("f64", "fx64"):
+        t64, nodes64 = 0.0, 0
+        for j in sample:
+            m = members[j]
+            lat = P.Lattice(m.nx, m.ny, m.omega, m.boundary, storage=storage).set_state(m.f0, m.rho0, m.u0)
+            lat.step(3)
+            k = 300
+            t64 += timed_ms(lambda: lat.step_graph(k, chunk=100)) / 1e3
+            nodes64 += m.nodes * k
+            del lat
+        rate = nodes64 / t64
+        seq[storage] = {"sequential_mlups": rate / 1e6, "sequential_wall_s_extrapolated": nodes * steps / rate,
+                        "speedup_of_batch": nodes * steps / rate / (ms / 1e3)}
     best = min(tune, key=lambda r: r["ms_per_step"])
     return {"workload": "%d von Karman lattices, %d steps each, %.1f M nodes, f16 storage" % (n, steps, nodes / 1e6),
             "aggregate_mlups": agg, "batch_wall_s": ms / 1e3, "autotuned": best,
-            "candidates": len(tune), "fx64_sequential_mlups": rate64 / 1e6,
-            "fx64_sequential_wall_s_extrapolated": seq_s, "speedup_vs_sequential_fx64": seq_s / (ms / 1e3),
+            "candidates": len(tune), "sequential": seq,
             "omega_range": [min(q["omega"] for q in params), max(q["omega"] for q in params)],
             "stability_risk_instances": sum(q["risky"] for q in params)}
 
@@ -192,12 +195,12 @@ def bench_batch(P, steps=20000, n=256):
 def bench_serve(P, n16=200, n64=40):
     """Serving: seeded Poisson arrivals at 50/s of Couette / Poiseuille / von
     Karman requests with 1k-50k steps, continuous batching under an HBM budget;
-    f16 storage against float64 accuracy (fx64 storage); error of f16 results
-    against their solo fx64 solve on a sample."""
+    f16 storage against plain float64 (f64 storage) and fx64; error of f16
+    results against their solo fx64 solve on a sample."""
     import torch
     from lattice_boltzmann_parallel_solver_gb300.serving import ServingEngine, request_mix, summarize
     out = {}
-    for storage, n in (("f16", n16), ("fx64", n64)):
+    for storage, n in (("f16", n16), ("fx64", n64), ("f64", n64)):
         reqs = request_mix(n, rate=50.0, seed=7)
         eng = ServingEngine(storage=storage, hbm_budget=64 << 30, tick_steps=500)
         done = eng.serve(reqs, realtime=True)
@@ -323,7 +326,9 @@ def reference_arm(args):
     core, each stepping its own cavity sample; aggregate MLUPS."""
     import multiprocessing as mp
     cores = os.cpu_count() or 1
-    n = 512 if args.steps <= 600 else 256
+    # per-process sample side: large enough to leave the caches, small enough
+    # that the whole --steps run stays within a few minutes
+    n = 512 if args.steps <= 600 else (256 if args.steps <= 3000 else 128)
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
         pool.map(_cpu_worker, [(64, 1, 0)] * cores)
@@ -443,13 +448,34 @@ def main():
             torch.cuda.empty_cache()
         extras["variants"] = variants
 
+        # the other cavity sizes of the bandwidth bench
+        sizes = {}
+        for m in (1024, 4096):
+            if m == n:
+                continue
+            bm = cavity_boundary_conditions(m, m, 0.1, 1.0)
+            sizes[str(m)] = {}
+            for st in ("fx64", "f64", "f32"):
+                k = min(args.steps, 2000)
+                lat_m = P.Lattice(m, m, 1.7, bm, storage=st).set_state(w.expand(m, m, 9).contiguous())
+                s_m, _ = timed(lat_m, k, 5)
+                s_m = slowest(s_m)
+                sizes[str(m)][st] = {"mlups": world * m * m * k / s_m / 1e6, "steps": k,
+                                     "hbm_frac": BYTES_PER_NODE[st] * m * m / (s_m / k) / 1e9 / hbm}
+                del lat_m
+            torch.cuda.empty_cache()
+        extras["cavity_sizes"] = sizes
+
         # end to end: the reference-facing drop-in call with pinned host buffers
         f_h = torch.empty((n, n, 9), dtype=torch.float64).pin_memory()
         f_h.copy_(w.cpu().expand(n, n, 9))
         rho_h = torch.ones((n, n), dtype=torch.float64).pin_memory()
         u_h = torch.zeros((n, n, 2), dtype=torch.float64).pin_memory()
-        e2e_steps = 5
+        e2e_steps = 10
+        # two untimed calls: the results of consecutive calls are both alive, so
+        # the pinned host allocator caches two sets of result buffers
         state = lattice_boltzmann_step(f_h, rho_h, u_h, 1.7, bnd)
+        state = lattice_boltzmann_step(*state, 1.7, bnd)
         barrier()
         t0 = time.perf_counter()
         for _ in range(e2e_steps):
