@@ -61,7 +61,7 @@ class Batch:
         self.storage = storage
         self.store_id, self.pop_dtype, self.aux_dtype = STORAGES[storage]
         self.device = torch.device(device)
-        self.npt = npt or (2 if storage in ("f64", "fx64") else 4)
+        self.npt = npt or {"fx64": 1, "f64": 2}.get(storage, 4)
         self.threads = threads
         self.blocks = blocks
         self.gbase = torch.zeros(1, dtype=torch.int32, device=self.device)
@@ -235,7 +235,7 @@ def autotune(batch: Batch, candidates=None, steps: int = 6, warmup: int = 2):
     (probes off) and the global step counter is reset afterwards."""
     sms = torch.cuda.get_device_properties(batch.device).multi_processor_count
     if candidates is None:
-        npts = (2, 4, 8) if batch.storage in ("f16", "bf16") else (2, 4)
+        npts = {"fx64": (1, 2), "f16": (2, 4, 8), "bf16": (2, 4, 8)}.get(batch.storage, (2, 4))
         candidates = [(p, t, b) for p in npts for t in (64, 128, 256) for b in (0, 2 * sms, 8 * sms)]
     best, results = None, []
     for npt, threads, blocks in candidates:

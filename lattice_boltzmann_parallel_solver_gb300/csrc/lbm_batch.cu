@@ -9,7 +9,7 @@
 namespace lbm {
 
 template <int STORE, int NPT, int THREADS>
-__global__ void __launch_bounds__(THREADS) batch_kernel(const BatchEntry* __restrict__ tab,
+__global__ void __launch_bounds__(THREADS, STORE == LBM_STORE_FX64 && NPT == 1 ? 1024 / THREADS : 1) batch_kernel(const BatchEntry* __restrict__ tab,
                                                         const int* __restrict__ tile_start, int n_inst,
                                                         int total_tiles, const int* __restrict__ gbase, int k) {
   const int g = *gbase + k;
@@ -54,8 +54,8 @@ int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_
   if (lat == nullptr || n < 1 || table == nullptr || total_tiles == nullptr)
     return set_error(LBM_ERR_ARG, "bad batch arguments");
   if (table_bytes < lbm_batch_table_bytes(n)) return set_error(LBM_ERR_ARG, "batch table buffer too small");
-  if (!(npt == 2 || npt == 4 || npt == 8) || !(threads == 64 || threads == 128 || threads == 256))
-    return set_error(LBM_ERR_ARG, "npt must be 2, 4 or 8 and threads 64, 128 or 256");
+  if (!(npt == 1 || npt == 2 || npt == 4 || npt == 8) || !(threads == 64 || threads == 128 || threads == 256))
+    return set_error(LBM_ERR_ARG, "npt must be 1, 2, 4 or 8 and threads 64, 128 or 256");
   if ((uintptr_t)table % 16 != 0) return set_error(LBM_ERR_ARG, "batch table must be 16-byte aligned");
   std::vector<BatchEntry> ent((size_t)n);
   std::vector<int> start((size_t)n);
@@ -150,8 +150,8 @@ extern "C" int lbm_batch_run(const void* table, int32_t n, int32_t total_tiles, 
 #define LBM_BATCH_NPT(ST, NP) LBM_BATCH_CASE(ST, NP, 64) LBM_BATCH_CASE(ST, NP, 128) LBM_BATCH_CASE(ST, NP, 256)
   LBM_BATCH_NPT(LBM_STORE_F64, 2)
   LBM_BATCH_NPT(LBM_STORE_F64, 4)
+  LBM_BATCH_NPT(LBM_STORE_FX64, 1)
   LBM_BATCH_NPT(LBM_STORE_FX64, 2)
-  LBM_BATCH_NPT(LBM_STORE_FX64, 4)
   LBM_BATCH_NPT(LBM_STORE_F32, 2)
   LBM_BATCH_NPT(LBM_STORE_F32, 4)
   LBM_BATCH_NPT(LBM_STORE_F16S, 2)

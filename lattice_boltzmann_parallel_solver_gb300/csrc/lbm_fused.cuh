@@ -317,6 +317,11 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
   for (int i = 0; i < 9; ++i) {
     const int row = cy(i) == 1 ? rm : (cy(i) == -1 ? rp : r0);
     const T* base = pin + i * plane + row;
+    if constexpr (NPT == 1) {
+      // one node per thread: the x neighbours come straight from L1
+      f[i][0] = __ldg(base + (cx(i) == 1 ? xm : (cx(i) == -1 ? xp : x0)));
+      continue;
+    }
     T v[NPT];
     ld_vec<T, NPT>(base + x0, v);
     if (cx(i) == 0) {
@@ -334,11 +339,13 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
 #pragma unroll
       for (int k = 0; k < NPT - 1; ++k) f[i][k] = v[k + 1];
       f[i][NPT - 1] = next;
-      if (nvalid < NPT) {
+      if constexpr (NPT > 1) {
+        if (nvalid < NPT) {
 #pragma unroll
-        for (int k = 0; k < NPT; ++k) {
-          const int xs = x0 + k + 1 < nx ? x0 + k + 1 : 0;
-          f[i][k] = __ldg(base + xs);
+          for (int k = 0; k < NPT; ++k) {
+            const int xs = x0 + k + 1 < nx ? x0 + k + 1 : 0;
+            f[i][k] = __ldg(base + xs);
+          }
         }
       }
     }
@@ -386,6 +393,7 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
 
   T pv[9];  // pressure rewrite computed by the node at column nx-2 or 1
   int pcol = -1;
+  const bool want_m = P.rho_out.p != nullptr || P.probe_buf != nullptr;
 #pragma unroll
   for (int k = 0; k < NPT; ++k) {
     int64_t g[9];
@@ -393,7 +401,7 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
     for (int i = 0; i < 9; ++i) g[i] = f[i][k];
     const int x = x0 + k;
     const bool pnode = HAS_PRESSURE && P.g.pressure && k < nvalid && (x == nx - 2 || x == 1);
-    const bool out = active && k < nvalid &&
+    const bool out = want_m && active && k < nvalid &&
                      (P.rho_out.p != nullptr || (P.probe_buf != nullptr && x == P.probe_x && y == P.probe_y));
     double rho = 1.0, ux = 0.0, uy = 0.0;
     if (out || pnode) {
@@ -438,7 +446,7 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
   if (!active) return;
   T* pout = static_cast<T*>(pop_out_v);
   const bool pr = HAS_PRESSURE && P.g.pressure;
-  if (nvalid == NPT && !(pr && (first || last))) {
+  if ((NPT == 1 || nvalid == NPT) && !(pr && (first || last))) {
 #pragma unroll
     for (int i = 0; i < 9; ++i) st_vec<T, NPT>(pout + i * plane + r0 + x0, f[i]);
   } else {

@@ -184,8 +184,9 @@ __global__ void __launch_bounds__(THREADS) fused_v2_kernel(const __grid_constant
                                                   (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y, P.seed);
 }
 
+// one node per thread: registers capped so that 1024 threads fit on an SM
 template <int NPT, int THREADS, bool HAS_BC, bool HAS_PRESSURE>
-__global__ void __launch_bounds__(THREADS) fused_fx_kernel(const __grid_constant__ KParams P) {
+__global__ void __launch_bounds__(THREADS, NPT == 1 ? 1024 / THREADS : 1) fused_fx_kernel(const __grid_constant__ KParams P) {
   fused_fx_body<NPT, HAS_BC, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out,
                                            (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y);
 }
@@ -264,8 +265,8 @@ static int launch_fx(const KParams& P, cudaStream_t s) {
 
 static int default_npt(int storage) {
   switch (storage) {
-    case LBM_STORE_F64:
-    case LBM_STORE_FX64: return 2;
+    case LBM_STORE_F64: return 2;
+    case LBM_STORE_FX64: return 1;
     case LBM_STORE_F32: return 4;
     default: return 4;
   }
@@ -285,6 +286,7 @@ static int launch_fused(int storage, int flags, const KParams& P, cudaStream_t s
   switch (storage * 16 + npt) {
     case LBM_STORE_F64 * 16 + 2: return launch_v2<LBM_STORE_F64, 2>(P, s);
     case LBM_STORE_F64 * 16 + 4: return launch_v2<LBM_STORE_F64, 4>(P, s);
+    case LBM_STORE_FX64 * 16 + 1: return launch_fx<1>(P, s);
     case LBM_STORE_FX64 * 16 + 2: return launch_fx<2>(P, s);
     case LBM_STORE_FX64 * 16 + 4: return launch_fx<4>(P, s);
     case LBM_STORE_F32 * 16 + 2: return launch_v2<LBM_STORE_F32, 2>(P, s);

@@ -42,7 +42,7 @@ def alone(pkg, m, storage, npt):
     return lat.set_state(m.f0, m.rho0, m.u0).step(m.steps)
 
 
-@pytest.mark.parametrize("storage,npt,threads", [("fx64", 2, 128), ("fx64", 4, 64), ("f64", 2, 128), ("f32", 4, 64), ("f16", 4, 128),
+@pytest.mark.parametrize("storage,npt,threads", [("fx64", 1, 128), ("fx64", 2, 64), ("f64", 2, 128), ("f32", 4, 64), ("f16", 4, 128),
                                                  ("f16", 8, 256), ("bf16", 2, 128)])
 def test_batch_members_equal_lone_runs(pkg, storage, npt, threads):
     from lattice_boltzmann_parallel_solver_gb300.batch import Batch

@@ -37,7 +37,7 @@ def start(nx, ny, seed):
 TOL = {"fx64": 1e-13, "f64": 1e-13, "f32": 1e-6, "f16": 1e-3, "bf16": 1e-2}
 
 
-@pytest.mark.parametrize("storage,npt", [("fx64", 2), ("fx64", 4), ("f64", 2), ("f64", 4), ("f32", 2), ("f32", 4), ("f16", 4),
+@pytest.mark.parametrize("storage,npt", [("fx64", 1), ("fx64", 2), ("fx64", 4), ("f64", 2), ("f64", 4), ("f32", 2), ("f32", 4), ("f16", 4),
                                          ("f16", 8), ("bf16", 4), ("bf16", 8)])
 @pytest.mark.parametrize("nx,ny", [(16, 9), (48, 20), (520, 12), (1040, 7)])
 def test_vectorised_matches_generic(pkg, storage, npt, nx, ny):
