@@ -91,12 +91,15 @@ template <> struct Store<LBM_STORE_F16S> {
   __device__ static A to_aux(R v, int) { return v; }
   __device__ static R from_aux(A a, int) { return a; }
   static constexpr bool kShifted = true;
-  __device__ static R dev(T t) { return __half2float(t) * kInv; }
-  __device__ static R ld_dev(const T* p) { return __half2float(__ldg(p)) * kInv; }
-  __device__ static T dev_rn(R d) { return __float2half_rn(d * kScale); }
-  // stochastic rounding with 13 random bits
+  // the vectorised kernel works on the stored, scaled deviation D = 1024 (f_i - w_i)
+  static constexpr float kDev = kScale;
+  __device__ static R dev(T t) { return __half2float(t); }
+  __device__ static R ld_dev(const T* p) { return __half2float(__ldg(p)); }
+  __device__ static T dev_rn(R d) { return __float2half_rn(d); }
+  // stochastic rounding: the top 13 bits of r, added below the 10 mantissa bits
+  // binary16 keeps, then truncation
   __device__ static T dev_sr(R d, uint32_t r) {
-    return __float2half_rz(__uint_as_float(__float_as_uint(d * kScale) + (r & 0x1FFFu)));
+    return __float2half_rz(__uint_as_float(__float_as_uint(d) + (r >> 19)));
   }
 };
 template <> struct Store<LBM_STORE_BF16S> {
@@ -110,12 +113,14 @@ template <> struct Store<LBM_STORE_BF16S> {
   __device__ static A to_aux(R v, int) { return v; }
   __device__ static R from_aux(A a, int) { return a; }
   static constexpr bool kShifted = true;
+  static constexpr float kDev = 1.0f;  // working deviation: f_i - w_i
   __device__ static R dev(T t) { return __bfloat162float(t); }
   __device__ static R ld_dev(const T* p) { return __bfloat162float(__ldg(p)); }
   __device__ static T dev_rn(R d) { return __float2bfloat16_rn(d); }
-  // stochastic rounding with 10 random bits added below the kept 16 bits
+  // stochastic rounding: the top 16 bits of r, added below the 16 bits bfloat16
+  // keeps, then truncation
   __device__ static T dev_sr(R d, uint32_t r) {
-    const uint32_t u = __float_as_uint(d) + ((r & 0x3FFu) << 6);
+    const uint32_t u = __float_as_uint(d) + (r >> 16);
     return __ushort_as_bfloat16((unsigned short)(u >> 16));
   }
 };
@@ -127,6 +132,15 @@ __host__ __device__ __forceinline__ uint32_t hash32(uint32_t x) {
   x *= 0x21f0aaadu;
   x ^= x >> 15;
   x *= 0x735a2d97u;
+  x ^= x >> 15;
+  return x;
+}
+
+// short integer mixer (xor-shift, multiply, xor-shift) for the per-node seed of
+// the stochastic rounding; a multiply-add step per direction follows it
+__host__ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
   x ^= x >> 15;
   return x;
 }
@@ -291,10 +305,10 @@ __device__ __forceinline__ void collide_fast(R f[9], R rho, R ux, R uy, R omega)
 #undef LBM_PAIR
 }
 
-// The same collision on deviations d_i = f_i - w_i (float32): with
-// drho = rho - 1 = sum d_i, d_i' = (1 - omega) d_i + omega w_i (drho + rho (4.5 cu^2 +- 3 cu - 1.5 |u|^2)).
-__device__ __forceinline__ void collide_dev(float d[9], float drho, float ux, float uy, float omega) {
-  const float rho = 1.0f + drho;
+// The same collision on scaled deviations d_i = s (f_i - w_i) (float32): with
+// sd = s (rho - 1) = sum d_i and srho = s rho = s + sd,
+// d_i' = (1 - omega) d_i + omega w_i (sd + srho (4.5 cu^2 +- 3 cu - 1.5 |u|^2)).
+__device__ __forceinline__ void collide_dev(float d[9], float drho, float rho, float ux, float uy, float omega) {
   const float om1 = 1.0f - omega;
   const float Bd = -1.5f * fmaf(ux, ux, uy * uy);
   const float orho = omega * rho, odr = omega * drho;

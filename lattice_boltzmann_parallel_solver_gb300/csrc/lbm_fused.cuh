@@ -89,8 +89,13 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
   using St = Store<STORE>;
   using T = typename St::T;
   using R = typename St::R;
-  // working values: deviations d = f - w for the shifted 16-bit storages, f otherwise
+  // working values: scaled deviations s (f - w) for the shifted 16-bit storages
+  // (the stored numbers themselves), f otherwise
   constexpr bool SH = St::kShifted;
+  constexpr R kS = [] {
+    if constexpr (SH) return (R)St::kDev;
+    else return R(1);
+  }();
   const int lane = threadIdx.x & 31;
   const int nx = P.g.nx, ny = P.g.ny;
   const int xlast = ((nx - 1) / NPT) * NPT;  // first node of the last chunk of a row
@@ -113,8 +118,8 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     if constexpr (SH) return St::dev(t);
     else return St::to_r(t, i);
   };
-  auto work_of_f = [&](R fv, int i) -> R { return SH ? fv - wr<R>(i) : fv; };
-  auto f_of_work = [&](R v, int i) -> R { return SH ? v + wr<R>(i) : v; };
+  auto work_of_f = [&](R fv, int i) -> R { return SH ? (fv - wr<R>(i)) * kS : fv; };
+  auto f_of_work = [&](R v, int i) -> R { return SH ? fma(v, R(1) / kS, wr<R>(i)) : v; };
 
   R f[9][NPT];
 #pragma unroll
@@ -167,7 +172,7 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
         for (int i = 0; i < 9; ++i) {
           const uint32_t s = (d >> (2 * i)) & 3u;
           if (s == LBM_SRC_BOUNCE)
-            f[i][k] = ld_work(pin + opp(i) * plane + r0 + x, opp(i)) - (R)P.g.kconst[ks][i];
+            f[i][k] = ld_work(pin + opp(i) * plane + r0 + x, opp(i)) - (R)P.g.kconst[ks][i] * kS;
           else if (s == LBM_SRC_CONST)
             f[i][k] = work_of_f((R)P.g.cconst[cs][i], i);
           else if (s == LBM_SRC_OUTLET && outlet_slot(i) >= 0 && aux_in != nullptr)
@@ -204,12 +209,12 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     const int x = x0 + k;
     const bool pnode = HAS_PRESSURE && P.g.pressure && k < nvalid && (x == nx - 2 || x == 1);
     const R sum = density9(g);
-    const R rho = SH ? R(1) + sum : sum;
+    const R rho = SH ? kS + sum : sum;  // s rho for the 16-bit storages
     R ux, uy;
     velocity_fast(g, rho, ux, uy);
     if (active && k < nvalid) {
       if (P.rho_out.p != nullptr) {
-        P.rho_out.p[x * P.rho_out.sx + y * P.rho_out.sy] = (double)rho;
+        P.rho_out.p[x * P.rho_out.sx + y * P.rho_out.sy] = SH ? 1.0 + (double)sum / (double)kS : (double)rho;
         double* up = P.u_out.p + x * P.u_out.sx + y * P.u_out.sy;
         up[0] = (double)ux;
         up[P.u_out.sc] = (double)uy;
@@ -217,13 +222,13 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
       write_probe(P, x, y, ux, uy);
     }
     if constexpr (SH)
-      collide_dev(g, sum, ux, uy, omega);
+      collide_dev(g, sum, rho, ux, uy, omega);
     else
       collide_fast(g, rho, ux, uy, omega);
     if (pnode) {
       R br[9];
       bracket9_fast(ux, uy, br);
-      const R rb = (R)(x == nx - 2 ? P.g.rho_in : P.g.rho_out) - rho;
+      const R rb = (R)(x == nx - 2 ? P.g.rho_in : P.g.rho_out) * kS - rho;
 #pragma unroll
       for (int i = 0; i < 9; ++i) pv[i] = fma(wr<R>(i) * br[i], rb, g[i]);
       pcol = x;
@@ -239,11 +244,11 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     if constexpr (SH) return sr ? St::dev_sr(v, rbits) : St::dev_rn(v);
     else return St::from_r(v, i);
   };
-  // random bits: one hash per node, then one multiply-add step per direction;
-  // each store takes 16 high bits
+  // random bits: one short hash per node, then one multiply-add step per
+  // direction; each store takes the high bits of the current word
   uint32_t hk[NPT];
 #pragma unroll
-  for (int k = 0; k < NPT; ++k) hk[k] = sr ? hash32((uint32_t)(y * nx + x0 + k) * 0x9E3779B1u ^ seed) : 0u;
+  for (int k = 0; k < NPT; ++k) hk[k] = sr ? mix32((uint32_t)(y * nx + x0 + k) * 0x9E3779B1u ^ seed) : 0u;
   T* pout = static_cast<T*>(pop_out_v);
   const bool pr = HAS_PRESSURE && P.g.pressure;
   if (nvalid == NPT && !(pr && (first || last))) {
@@ -252,7 +257,7 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
       T raw[NPT];
 #pragma unroll
       for (int k = 0; k < NPT; ++k) {
-        raw[k] = to_store(f[i][k], i, hk[k] >> 16);
+        raw[k] = to_store(f[i][k], i, hk[k]);
         hk[k] = hk[k] * 0x2C1B3C6Du + 0x297A2D39u;
       }
       st_vec<T, NPT>(pout + i * plane + r0 + x0, raw);
@@ -267,7 +272,7 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
         const int x = x0 + k;
         const bool skip = k >= nvalid || (pr && ((x == 0 && ((P.g.pin >> i) & 1u)) ||
                                                  (x == nx - 1 && ((P.g.pout >> i) & 1u))));
-        if (!skip) pout[i * plane + r0 + x] = to_store(f[i][k], i, hk[k] >> 16);
+        if (!skip) pout[i * plane + r0 + x] = to_store(f[i][k], i, hk[k]);
         hk[k] = hk[k] * 0x2C1B3C6Du + 0x297A2D39u;
       }
     }
@@ -275,10 +280,10 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
   if (pr && pcol >= 0) {
     const uint32_t dirs = pcol == nx - 2 ? P.g.pin : P.g.pout;
     const int dst = pcol == nx - 2 ? 0 : nx - 1;
-    uint32_t hp = sr ? hash32((uint32_t)(y * nx + dst) * 0x9E3779B1u ^ seed ^ 0x5bd1e995u) : 0u;
+    uint32_t hp = sr ? mix32((uint32_t)(y * nx + dst) * 0x9E3779B1u ^ seed ^ 0x5bd1e995u) : 0u;
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
-      if ((dirs >> i) & 1u) pout[i * plane + r0 + dst] = to_store(pv[i], i, hp >> 16);
+      if ((dirs >> i) & 1u) pout[i * plane + r0 + dst] = to_store(pv[i], i, hp);
       hp = hp * 0x2C1B3C6Du + 0x297A2D39u;
     }
   }

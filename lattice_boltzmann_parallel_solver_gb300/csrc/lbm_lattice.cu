@@ -178,8 +178,10 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
   }
 }
 
+// the 16-bit storages are issue-bound: registers capped so that 1024 threads fit on an SM
 template <int STORE, int NPT, int THREADS, bool HAS_BC, bool HAS_PRESSURE>
-__global__ void __launch_bounds__(THREADS) fused_v2_kernel(const __grid_constant__ KParams P) {
+__global__ void __launch_bounds__(THREADS, (STORE == LBM_STORE_F16S || STORE == LBM_STORE_BF16S) ? 1024 / THREADS : 1)
+    fused_v2_kernel(const __grid_constant__ KParams P) {
   fused_v2_body<STORE, NPT, HAS_BC, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out,
                                                   (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y, P.seed);
 }
