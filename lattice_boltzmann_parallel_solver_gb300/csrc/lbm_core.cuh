@@ -199,6 +199,15 @@ template <typename R>
 __device__ __forceinline__ R density9(const R f[9]) {
   return (((f[0] + f[1]) + (f[2] + f[3])) + ((f[4] + f[5]) + (f[6] + f[7]))) + f[8];
 }
+// sum f_i and j = sum c_i f_i with shared partial sums (14 additions instead of 18)
+template <typename R>
+__device__ __forceinline__ void moments9(const R f[9], R& sum, R& jx, R& jy) {
+  const R a = (f[1] + f[5]) + f[8], b = (f[3] + f[6]) + f[7];
+  const R c = (f[2] + f[5]) + f[6], e = (f[4] + f[7]) + f[8];
+  jx = a - b;
+  jy = c - e;
+  sum = ((f[0] + f[2]) + (a + b)) + f[4];
+}
 __device__ __forceinline__ double density9_exact(const double f[9]) {
   double a = __dadd_rn(__dadd_rn(f[0], f[1]), __dadd_rn(f[2], f[3]));
   double b = __dadd_rn(__dadd_rn(f[4], f[5]), __dadd_rn(f[6], f[7]));

@@ -201,6 +201,7 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
   R pv[9];  // pressure rewrite computed by the node at column nx-2 or 1
   int pcol = -1;
   const R omega = (R)P.omega;
+  const bool want_m = P.rho_out.p != nullptr || P.probe_buf != nullptr;
 #pragma unroll
   for (int k = 0; k < NPT; ++k) {
     R g[9];
@@ -208,11 +209,12 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     for (int i = 0; i < 9; ++i) g[i] = f[i][k];
     const int x = x0 + k;
     const bool pnode = HAS_PRESSURE && P.g.pressure && k < nvalid && (x == nx - 2 || x == 1);
-    const R sum = density9(g);
+    R sum, jx, jy;
+    moments9(g, sum, jx, jy);
     const R rho = SH ? kS + sum : sum;  // s rho for the 16-bit storages
-    R ux, uy;
-    velocity_fast(g, rho, ux, uy);
-    if (active && k < nvalid) {
+    const R inv = rho != R(0) ? rcp_nr(rho) : R(0);
+    const R ux = jx * inv, uy = jy * inv;
+    if (want_m && active && k < nvalid) {
       if (P.rho_out.p != nullptr) {
         P.rho_out.p[x * P.rho_out.sx + y * P.rho_out.sy] = SH ? 1.0 + (double)sum / (double)kS : (double)rho;
         double* up = P.u_out.p + x * P.u_out.sx + y * P.u_out.sy;

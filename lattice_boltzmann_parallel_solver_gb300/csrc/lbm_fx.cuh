@@ -194,9 +194,10 @@ DF_HD bool collide_q(int64_t d[9], const QConsts& c) {
   uint32_t big = 0;  // |d_i| < 2^54: (hi32 + 2^22) < 2^23 for all i
 #pragma unroll
   for (int i = 0; i < 9; ++i) big |= (uint32_t)hi32(d[i]) + (1u << 22);
-  const int64_t D = ((d[0] + d[1]) + (d[2] + d[3])) + ((d[4] + d[5]) + (d[6] + d[7])) + d[8];
-  const int64_t jx = (d[1] + d[5] + d[8]) - (d[3] + d[6] + d[7]);
-  const int64_t jy = (d[2] + d[5] + d[6]) - (d[4] + d[7] + d[8]);
+  const int64_t pa = d[1] + d[5] + d[8], pb = d[3] + d[6] + d[7];
+  const int64_t pc = d[2] + d[5] + d[6], pe = d[4] + d[7] + d[8];
+  const int64_t D = (d[0] + d[2] + d[4]) + (pa + pb);
+  const int64_t jx = pa - pb, jy = pc - pe;
   // |rho - 1| < 1
   if ((big >> 23) != 0u || (uint32_t)hi32(D) + (1u << 24) >= (1u << 25)) return false;
   const df::F2 Dq = q_to_f2(D), X = q_to_f2(jx), Y = q_to_f2(jy);
