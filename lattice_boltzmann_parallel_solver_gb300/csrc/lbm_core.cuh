@@ -341,6 +341,46 @@ __device__ __forceinline__ void collide_dev(float d[9], float drho, float rho, f
 #undef LBM_DPAIR
 }
 
+// ---- two nodes per instruction: packed float32 pairs (sm_100 family) --------
+__device__ __forceinline__ float2 f2c(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2c(-1.0f), a); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+
+__device__ __forceinline__ void moments9x2(const float2 f[9], float2& sum, float2& jx, float2& jy) {
+  const float2 a = add2(add2(f[1], f[5]), f[8]), b = add2(add2(f[3], f[6]), f[7]);
+  const float2 c = add2(add2(f[2], f[5]), f[6]), e = add2(add2(f[4], f[7]), f[8]);
+  jx = sub2(a, b);
+  jy = sub2(c, e);
+  sum = add2(add2(add2(f[0], f[2]), add2(a, b)), f[4]);
+}
+
+// collide_dev on two nodes at once
+__device__ __forceinline__ void collide_dev2(float2 d[9], float2 drho, float2 rho, float2 ux, float2 uy, float omega) {
+  const float2 om1 = f2c(1.0f - omega), om = f2c(omega);
+  const float2 Bd = mul2(f2c(-1.5f), fma2(ux, ux, mul2(uy, uy)));
+  const float2 orho = mul2(om, rho), odr = mul2(om, drho);
+  const float2 W0 = mul2(orho, f2c(wf(0))), W1 = mul2(orho, f2c(wf(1))), W5 = mul2(orho, f2c(wf(5)));
+  const float2 D0 = mul2(odr, f2c(wf(0))), D1 = mul2(odr, f2c(wf(1))), D5 = mul2(odr, f2c(wf(5)));
+  const float2 V1 = mul2(f2c(3.0f), W1), V5 = mul2(f2c(3.0f), W5);
+  d[0] = fma2(om1, d[0], fma2(W0, Bd, D0));
+  const float2 d58 = add2(ux, uy), d67 = sub2(uy, ux);
+#define LBM_DPAIR2(I, J, V, W, D, VV)                  \
+  {                                                   \
+    const float2 t = fma2(mul2(f2c(4.5f), (V)), (V), Bd); \
+    const float2 s = fma2((W), t, (D));               \
+    const float2 m = mul2((VV), (V));                 \
+    d[I] = fma2(om1, d[I], add2(s, m));               \
+    d[J] = fma2(om1, d[J], sub2(s, m));               \
+  }
+  LBM_DPAIR2(1, 3, ux, W1, D1, V1)
+  LBM_DPAIR2(2, 4, uy, W1, D1, V1)
+  LBM_DPAIR2(5, 7, d58, W5, D5, V5)
+  LBM_DPAIR2(6, 8, d67, W5, D5, V5)
+#undef LBM_DPAIR2
+}
+
 // equilibrium with FMAs (used where the fast path needs feq itself)
 template <typename R>
 __device__ __forceinline__ void bracket9_fast(R ux, R uy, R br[9]) {

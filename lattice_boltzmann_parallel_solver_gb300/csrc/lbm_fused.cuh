@@ -202,18 +202,10 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
   int pcol = -1;
   const R omega = (R)P.omega;
   const bool want_m = P.rho_out.p != nullptr || P.probe_buf != nullptr;
-#pragma unroll
-  for (int k = 0; k < NPT; ++k) {
-    R g[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) g[i] = f[i][k];
+  // moments written out for the last step or the probe, and the pressure
+  // rewrite source, of node k (working values g after the collision)
+  auto node_extras = [&](int k, R sum, R rho, R ux, R uy, const R g[9]) {
     const int x = x0 + k;
-    const bool pnode = HAS_PRESSURE && P.g.pressure && k < nvalid && (x == nx - 2 || x == 1);
-    R sum, jx, jy;
-    moments9(g, sum, jx, jy);
-    const R rho = SH ? kS + sum : sum;  // s rho for the 16-bit storages
-    const R inv = rho != R(0) ? rcp_nr(rho) : R(0);
-    const R ux = jx * inv, uy = jy * inv;
     if (want_m && active && k < nvalid) {
       if (P.rho_out.p != nullptr) {
         P.rho_out.p[x * P.rho_out.sx + y * P.rho_out.sy] = SH ? 1.0 + (double)sum / (double)kS : (double)rho;
@@ -223,11 +215,7 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
       }
       write_probe(P, x, y, ux, uy);
     }
-    if constexpr (SH)
-      collide_dev(g, sum, rho, ux, uy, omega);
-    else
-      collide_fast(g, rho, ux, uy, omega);
-    if (pnode) {
+    if (HAS_PRESSURE && P.g.pressure && k < nvalid && (x == nx - 2 || x == 1)) {
       R br[9];
       bracket9_fast(ux, uy, br);
       const R rb = (R)(x == nx - 2 ? P.g.rho_in : P.g.rho_out) * kS - rho;
@@ -235,8 +223,50 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
       for (int i = 0; i < 9; ++i) pv[i] = fma(wr<R>(i) * br[i], rb, g[i]);
       pcol = x;
     }
+  };
+  if constexpr (SH && NPT % 2 == 0) {
+    // 16-bit storages: two nodes per packed float32 instruction
 #pragma unroll
-    for (int i = 0; i < 9; ++i) f[i][k] = g[i];
+    for (int k = 0; k < NPT; k += 2) {
+      float2 g2[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) g2[i] = make_float2(f[i][k], f[i][k + 1]);
+      float2 sum, jx, jy;
+      moments9x2(g2, sum, jx, jy);
+      const float2 rho = add2(f2c(kS), sum);  // s rho
+      const float2 inv = make_float2(rho.x != 0.0f ? rcp_nr(rho.x) : 0.0f, rho.y != 0.0f ? rcp_nr(rho.y) : 0.0f);
+      const float2 ux = mul2(jx, inv), uy = mul2(jy, inv);
+      collide_dev2(g2, sum, rho, ux, uy, omega);
+      R ga[9], gb[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) {
+        ga[i] = g2[i].x;
+        gb[i] = g2[i].y;
+        f[i][k] = ga[i];
+        f[i][k + 1] = gb[i];
+      }
+      node_extras(k, sum.x, rho.x, ux.x, uy.x, ga);
+      node_extras(k + 1, sum.y, rho.y, ux.y, uy.y, gb);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < NPT; ++k) {
+      R g[9];
+#pragma unroll
+      for (int i = 0; i < 9; ++i) g[i] = f[i][k];
+      R sum, jx, jy;
+      moments9(g, sum, jx, jy);
+      const R rho = SH ? kS + sum : sum;  // s rho for the 16-bit storages
+      const R inv = rho != R(0) ? rcp_nr(rho) : R(0);
+      const R ux = jx * inv, uy = jy * inv;
+      if constexpr (SH)
+        collide_dev(g, sum, rho, ux, uy, omega);
+      else
+        collide_fast(g, rho, ux, uy, omega);
+      node_extras(k, sum, rho, ux, uy, g);
+#pragma unroll
+      for (int i = 0; i < 9; ++i) f[i][k] = g[i];
+    }
   }
 
   if (!active) return;
