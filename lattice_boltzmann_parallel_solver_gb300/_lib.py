@@ -72,6 +72,8 @@ SIGNATURES = {
     "lbm_halo_fill_f64": (C.c_int, [vp, i32, i32, vp]),
     "lbm_step_scratch_bytes": (C.c_size_t, [i32, i32]),
     "lbm_step_f64": (C.c_int, [GP, vp, vp, vp, f64, vp, vp, vp, vp, i32, vp]),
+    "lbm_step_host_scratch_bytes": (C.c_size_t, [i32, i32]),
+    "lbm_step_f64_host": (C.c_int, [GP, vp, vp, vp, f64, vp, vp, vp, vp, C.c_size_t, i32, i32, vp]),
     "lbm_step_f64_noalloc": (C.c_int, [GP, vp, vp, vp, f64, vp, vp, vp, i32, vp]),
     "lbm_lattice_pop_bytes": (C.c_size_t, [i32, i32, i64, i32]),
     "lbm_lattice_init": (C.c_int, [GP, i32, vp, vp, vp, f64, vp, i64, vp, i32, vp]),

@@ -36,6 +36,8 @@ struct OutView {
 
 struct KParams {
   GeoK g;
+  // columns [xb, xe) handled by the one-node-per-thread kernel (xe == 0: all)
+  int xb, xe;
   const void* pop_in;
   void* pop_out;
   int64_t pitch, plane;

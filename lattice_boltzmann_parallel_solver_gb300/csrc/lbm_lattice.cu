@@ -27,10 +27,10 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
   using St = Store<STORE>;
   using T = typename St::T;
   using R = typename St::R;
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  const int y = blockIdx.y * blockDim.y + threadIdx.y;
   const int nx = P.g.nx, ny = P.g.ny;
-  if (x >= nx || y >= ny) return;
+  const int x = P.xb + blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= (P.xe > 0 ? P.xe : nx) || y >= ny) return;
   const int64_t r0 = (int64_t)y * P.pitch;
   using A = typename St::A;
   const A* aux_in = static_cast<const A*>(P.aux_in);
@@ -206,7 +206,7 @@ static void launch_dims(int nx, int ny, dim3& grid, dim3& block) {
 template <int STORE, bool EXACT, int MODE>
 static int launch(const KParams& P, cudaStream_t s) {
   dim3 grid, block;
-  launch_dims(P.g.nx, P.g.ny, grid, block);
+  launch_dims((P.xe > 0 ? P.xe : P.g.nx) - P.xb, P.g.ny, grid, block);
   lattice_kernel<STORE, EXACT, MODE><<<grid, block, 0, s>>>(P);
   count_launch();
   return check_launch("lattice_kernel");
@@ -438,5 +438,142 @@ int lbm_step_f64(const lbm_geometry* g, const double* f, const double* rho, cons
                                   : launch<LBM_STORE_F64, false, MODE_READ>(P, (cudaStream_t)stream);
 }
 
+// ---- the drop-in step on host buffers, with copies and kernels overlapped ----
+size_t lbm_step_host_scratch_bytes(int32_t nx, int32_t ny) {
+  const int64_t pitch = ((int64_t)nx + 31) / 32 * 32, n = (int64_t)nx * ny;
+  return (size_t)(24 * n + 9 * pitch * ny + 3 * (int64_t)ny) * sizeof(double) + 4 * 256;
+}
+
+int lbm_step_f64_host(const lbm_geometry* g, const double* f, const double* rho, const double* u, double omega,
+                      double* f_out, double* rho_out, double* u_out, void* scratch, size_t scratch_bytes,
+                      int32_t flags, int32_t slabs, void* stream) {
+  if (g == nullptr) return set_error(LBM_ERR_ARG, "geometry is NULL");
+  if (f == nullptr || rho == nullptr || u == nullptr || f_out == nullptr || rho_out == nullptr ||
+      u_out == nullptr || scratch == nullptr)
+    return set_error(LBM_ERR_ARG, "f, rho, u, f_out, rho_out, u_out and scratch are required");
+  KParams G;
+  std::memset(&G, 0, sizeof(G));
+  if (!to_geok(g, G.g)) return last_status();
+  if (int e = check_omega(omega)) return e;
+  const int nx = g->nx, ny = g->ny;
+  if (scratch_bytes < lbm_step_host_scratch_bytes(nx, ny)) return set_error(LBM_ERR_ARG, "scratch too small");
+  const int64_t n = (int64_t)nx * ny, pitch = ((int64_t)nx + 31) / 32 * 32;
+  const bool exact = (flags & LBM_FLAG_EXACT) != 0;
+  // device layout: inputs f, rho, u | outputs f, rho, u | populations | outlet memory
+  double* base = reinterpret_cast<double*>(((uintptr_t)scratch + 255) & ~(uintptr_t)255);
+  double* fin = base;
+  double* rin = fin + 9 * n;
+  double* uin = rin + n;
+  double* fo = uin + 2 * n;
+  double* ro = fo + 9 * n;
+  double* uo = ro + n;
+  double* pop = reinterpret_cast<double*>(((uintptr_t)(uo + 2 * n) + 255) & ~(uintptr_t)255);
+  double* aux = pop + 9 * pitch * ny;
+  const int K = std::max(1, std::min(slabs > 0 ? slabs : 8, nx));
+  auto xs = [&](int k) { return (int)((int64_t)k * nx / K); };
+  cudaStream_t caller = (cudaStream_t)stream, sh = nullptr, sc = nullptr, sd = nullptr;
+  std::vector<cudaEvent_t> ev;
+  int st = LBM_OK;
+  auto cuda_ok = [&](cudaError_t e) {
+    if (e != cudaSuccess && st == LBM_OK) st = set_error(LBM_ERR_CUDA, cudaGetErrorString(e));
+    return st == LBM_OK;
+  };
+  auto event = [&]() {
+    cudaEvent_t e = nullptr;
+    cuda_ok(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    ev.push_back(e);
+    return e;
+  };
+  cuda_ok(cudaStreamCreateWithFlags(&sh, cudaStreamNonBlocking));
+  cuda_ok(cudaStreamCreateWithFlags(&sc, cudaStreamNonBlocking));
+  cuda_ok(cudaStreamCreateWithFlags(&sd, cudaStreamNonBlocking));
+  cudaEvent_t start = event();
+  cuda_ok(cudaEventRecord(start, caller));
+  cuda_ok(cudaStreamWaitEvent(sh, start, 0));
+  cuda_ok(cudaStreamWaitEvent(sc, start, 0));
+  cuda_ok(cudaStreamWaitEvent(sd, start, 0));
+  std::vector<cudaEvent_t> in_ready(K), out_ready(K);
+  for (int k = 0; k < K && st == LBM_OK; ++k) {
+    const int64_t a = xs(k), w = xs(k + 1) - xs(k);
+    cuda_ok(cudaMemcpyAsync(fin + 9 * a * ny, f + 9 * a * ny, 9 * w * ny * sizeof(double), cudaMemcpyHostToDevice, sh));
+    cuda_ok(cudaMemcpyAsync(rin + a * ny, rho + a * ny, w * ny * sizeof(double), cudaMemcpyHostToDevice, sh));
+    cuda_ok(cudaMemcpyAsync(uin + 2 * a * ny, u + 2 * a * ny, 2 * w * ny * sizeof(double), cudaMemcpyHostToDevice, sh));
+    in_ready[k] = event();
+    cuda_ok(cudaEventRecord(in_ready[k], sh));
+  }
+  auto init = [&](int k) {
+    KParams P = G;
+    P.xb = xs(k);
+    P.xe = xs(k + 1);
+    P.pop_out = pop;
+    P.pitch = pitch;
+    P.plane = pitch * ny;
+    P.aux_out = aux;
+    P.f_in = ref_f(fin, ny);
+    P.rho_in = ref_rho(rin, ny);
+    P.u_in = ref_u(uin, ny);
+    P.omega = omega;
+    if (!cuda_ok(cudaStreamWaitEvent(sc, in_ready[k], 0))) return;
+    const int e = exact ? launch<LBM_STORE_F64, true, MODE_INIT>(P, sc) : launch<LBM_STORE_F64, false, MODE_INIT>(P, sc);
+    if (e != LBM_OK && st == LBM_OK) st = e;
+  };
+  std::vector<int> order;  // slabs in the order they are read out
+  auto read = [&](int k) {
+    KParams P = G;
+    P.xb = xs(k);
+    P.xe = xs(k + 1);
+    P.pop_in = pop;
+    P.aux_in = aux;
+    P.pitch = pitch;
+    P.plane = pitch * ny;
+    P.f_out = ref_f_out(fo, ny);
+    P.rho_out = ref_rho_out(ro, ny);
+    P.u_out = ref_u_out(uo, ny);
+    const int e = exact ? launch<LBM_STORE_F64, true, MODE_READ>(P, sc) : launch<LBM_STORE_F64, false, MODE_READ>(P, sc);
+    if (e != LBM_OK && st == LBM_OK) st = e;
+    out_ready[k] = event();
+    cuda_ok(cudaEventRecord(out_ready[k], sc));
+    order.push_back(k);
+  };
+  // Read-out of slab k pulls from columns of slabs k-1 and k+1 (periodic in x),
+  // so it follows their collisions.  The pressure rewrite writes columns 0 and
+  // nx-1 from columns nx-2 and 1: with it, every collision runs first.
+  if (g->pressure || K < 3) {
+    for (int k = 0; k < K; ++k) init(k);
+    for (int k = 0; k < K; ++k) read(k);
+  } else {
+    init(0);
+    init(1);
+    for (int k = 2; k < K; ++k) {
+      init(k);
+      read(k - 1);
+    }
+    read(K - 1);
+    read(0);
+  }
+  for (int k : order) {
+    if (st != LBM_OK) break;
+    const int64_t a = xs(k), w = xs(k + 1) - xs(k);
+    cuda_ok(cudaStreamWaitEvent(sd, out_ready[k], 0));
+    cuda_ok(cudaMemcpyAsync(f_out + 9 * a * ny, fo + 9 * a * ny, 9 * w * ny * sizeof(double), cudaMemcpyDeviceToHost, sd));
+    cuda_ok(cudaMemcpyAsync(rho_out + a * ny, ro + a * ny, w * ny * sizeof(double), cudaMemcpyDeviceToHost, sd));
+    cuda_ok(cudaMemcpyAsync(u_out + 2 * a * ny, uo + 2 * a * ny, 2 * w * ny * sizeof(double), cudaMemcpyDeviceToHost, sd));
+  }
+  // the caller's stream continues once every copy has landed
+  cudaEvent_t done_h = event(), done_c = event(), done_d = event();
+  cuda_ok(cudaEventRecord(done_h, sh));
+  cuda_ok(cudaEventRecord(done_c, sc));
+  cuda_ok(cudaEventRecord(done_d, sd));
+  cuda_ok(cudaStreamWaitEvent(caller, done_h, 0));
+  cuda_ok(cudaStreamWaitEvent(caller, done_c, 0));
+  cuda_ok(cudaStreamWaitEvent(caller, done_d, 0));
+  // streams and events are released once their work completes
+  for (cudaEvent_t e : ev)
+    if (e) cudaEventDestroy(e);
+  if (sh) cudaStreamDestroy(sh);
+  if (sc) cudaStreamDestroy(sc);
+  if (sd) cudaStreamDestroy(sd);
+  return st;
+}
 
 }  // extern "C"

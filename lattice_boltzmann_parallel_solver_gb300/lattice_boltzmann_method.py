@@ -119,15 +119,40 @@ def collision(f, density, velocity, omega, exact=True):
 _SCRATCH = {}
 
 
-def _scratch(nx, ny, device):
-    key = (nx, ny, str(device))
+def _scratch(nx, ny, device, host=False):
+    key = (nx, ny, str(device), host)
     t = _SCRATCH.get(key)
     if t is None:
-        n = int(_lib.load().lbm_step_scratch_bytes(nx, ny))
-        t = torch.empty(n, dtype=torch.uint8, device=device)
+        lib = _lib.load()
+        n = int(lib.lbm_step_host_scratch_bytes(nx, ny) if host else lib.lbm_step_scratch_bytes(nx, ny))
         _SCRATCH.clear()
+        t = torch.empty(n, dtype=torch.uint8, device=device)
         _SCRATCH[key] = t
     return t
+
+
+def _host_f64(a) -> torch.Tensor:
+    """Contiguous float64 CPU tensor viewing ``a`` where it can (NumPy arrays
+    are not copied; pinned tensors stay pinned, which lets the copies overlap)."""
+    t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a, dtype=np.float64))
+    return t.to(torch.float64).contiguous()
+
+
+def _step_host(geo, f, rho, u, omega, flags, kind, slabs=0):
+    """The fused step on host arrays: slabs of x copied in, stepped and copied
+    out with the copies and kernels overlapped (lbm_step_f64_host; ``slabs`` 0
+    takes its default)."""
+    fh, rh, uh = _host_f64(f), _host_f64(rho), _host_f64(u)
+    assert tuple(fh.shape[0:2]) == tuple(rh.shape) and tuple(fh.shape[0:2]) == tuple(uh.shape[0:2])
+    assert fh.dim() == 3 and fh.shape[-1] == 9
+    nx, ny = int(fh.shape[0]), int(fh.shape[1])
+    outs = [torch.empty(t.shape, dtype=torch.float64, pin_memory=True) for t in (fh, rh, uh)]
+    scratch = _scratch(nx, ny, torch.device("cuda"), host=True)
+    _lib.call("lbm_step_f64_host", geo.ref, fh.data_ptr(), rh.data_ptr(), uh.data_ptr(), float(omega),
+              outs[0].data_ptr(), outs[1].data_ptr(), outs[2].data_ptr(), scratch.data_ptr(), scratch.numel(),
+              flags, int(slabs), A.stream())
+    torch.cuda.current_stream().synchronize()
+    return tuple(o if kind == A.TORCH_CPU else o.numpy() for o in outs)
 
 
 def _is_own_hook(obj) -> bool:
@@ -149,12 +174,30 @@ def lattice_boltzmann_step(f, density, velocity, omega, boundary=None, parallel_
 
     ``boundary`` built by this package's factories (boundary_utils, or
     ``Boundary([...])``) and no halo hook run fused: two kernels for the whole
-    step.  Any other callable, or a halo hook, runs the unfused sequence
-    collide -> hook -> stream -> boundary -> moments on device arrays.
+    step; on host arrays (NumPy, CPU tensors) the copies in and out are cut
+    into slabs of x and overlapped with the kernels.  Any other callable, or a
+    halo hook, runs the unfused sequence collide -> hook -> stream -> boundary
+    -> moments on device arrays.
     ``exact=True`` (the default) keeps NumPy's float64 operation order, so the
     result is bit-for-bit the reference's; ``exact=False`` uses the FMA form.
     """
     kind = A.kind_of(f)
+    assert 0 < omega < 2
+    if kind != A.TORCH_CUDA and parallel_communication is None:
+        # host arrays and a fusable boundary: the pipelined host-buffer step
+        A.require_cuda()
+        shp = np.shape(f)
+        assert len(shp) == 3 and shp[-1] == 9
+        nx, ny = int(shp[0]), int(shp[1])
+        if boundary is None:
+            hgeo = empty_geometry(nx, ny)
+        elif _is_own_hook(boundary) and hasattr(boundary, "geometry"):
+            hgeo = boundary.geometry(nx, ny)
+            hgeo = hgeo if hgeo.fusable else None
+        else:
+            hgeo = None
+        if hgeo is not None:
+            return _step_host(hgeo, f, density, velocity, omega, _lib.FLAG_EXACT if exact else 0, kind)
     ft, rho, u = A.to_device(f), A.to_device(density), A.to_device(velocity)
     assert tuple(ft.shape[0:2]) == tuple(rho.shape)
     assert tuple(ft.shape[0:2]) == tuple(u.shape[0:2])
