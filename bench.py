@@ -487,7 +487,7 @@ def main():
         extras["e2e"] = {"value": world * nodes * e2e_steps / e2e_secs / 1e6, "unit": "MLUPS",
                          "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io,
                          "path": "lattice_boltzmann_step(f, rho, u, omega, boundary) on pinned host tensors, "
-                                 "exact float64, %d steps" % e2e_steps}
+                                 "exact float64, %d steps (slab-pipelined copies, lbm_step_f64_host)" % e2e_steps}
         del f_h, rho_h, u_h, state
         if rank == 0 and world == 1:
             extras["cpu_baseline"] = cpu_baseline_single()

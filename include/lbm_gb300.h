@@ -123,12 +123,13 @@ int lbm_step_f64(const lbm_geometry* g, const double* f, const double* rho, cons
 
 /* The same step on HOST buffers in the reference layout (what the reference's
  * drivers hold: NumPy arrays; pinned memory lets the copies run asynchronously).
- * The lattice is cut into `slabs` ranges of x (0 = 8), which are contiguous in
- * the reference layout: slab k+1 is copied in while slab k is collided and
- * streamed and slab k-1 is copied out, on three internal streams, so the two
- * copy directions and the kernels overlap.  The caller's `stream` waits for all
- * of it.  `scratch` must hold lbm_step_host_scratch_bytes(nx, ny) bytes
- * (device).  Results are identical to lbm_step_f64's. */
+ * The lattice is cut into `slabs` ranges of x (0: one per 2^18 nodes, at most
+ * 32), which are contiguous in the reference layout: slab k+1 is copied in
+ * while slab k is collided and streamed and slab k-1 is copied out, on three
+ * internal streams, so the two copy directions and the kernels overlap.  The
+ * caller's `stream` waits for all of it.  `scratch` must hold
+ * lbm_step_host_scratch_bytes(nx, ny) bytes (device).  Results are identical
+ * to lbm_step_f64's. */
 size_t lbm_step_host_scratch_bytes(int32_t nx, int32_t ny);
 int lbm_step_f64_host(const lbm_geometry* g, const double* f, const double* rho, const double* u,
                       double omega, double* f_out, double* rho_out, double* u_out, void* scratch,

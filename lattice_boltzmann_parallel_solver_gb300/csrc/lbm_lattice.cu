@@ -469,7 +469,10 @@ int lbm_step_f64_host(const lbm_geometry* g, const double* f, const double* rho,
   double* uo = ro + n;
   double* pop = reinterpret_cast<double*>(((uintptr_t)(uo + 2 * n) + 255) & ~(uintptr_t)255);
   double* aux = pop + 9 * pitch * ny;
-  const int K = std::max(1, std::min(slabs > 0 ? slabs : 8, nx));
+  // default depth: one slab per 2^18 nodes, at most 32 (the copies then run
+  // within a few percent of the link's two-way rate on large lattices)
+  const int64_t auto_k = std::max<int64_t>(1, std::min<int64_t>(32, n >> 18));
+  const int K = (int)std::max<int64_t>(1, std::min<int64_t>(slabs > 0 ? slabs : auto_k, nx));
   auto xs = [&](int k) { return (int)((int64_t)k * nx / K); };
   cudaStream_t caller = (cudaStream_t)stream, sh = nullptr, sc = nullptr, sd = nullptr;
   std::vector<cudaEvent_t> ev;
