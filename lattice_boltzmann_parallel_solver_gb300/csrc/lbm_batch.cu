@@ -8,32 +8,65 @@
 
 namespace lbm {
 
+// Tiles are handed out in groups of kTileGroup consecutive tiles (mostly of one
+// lattice), so the owner search and the entry's cache lines are shared by the
+// group; groups are strided over the persistent grid.
+constexpr int kTileGroup = 8;
+
+// registers capped so that 768 threads fit on an SM (the body with every
+// boundary form compiled in needs more than the single-lattice kernels' 64)
 template <int STORE, int NPT, int THREADS>
-__global__ void __launch_bounds__(THREADS, STORE == LBM_STORE_FX64 && NPT == 1 ? 1024 / THREADS : 1) batch_kernel(const BatchEntry* __restrict__ tab,
-                                                        const int* __restrict__ tile_start, int n_inst,
-                                                        int total_tiles, const int* __restrict__ gbase, int k) {
+__global__ void __launch_bounds__(THREADS, (STORE == LBM_STORE_FX64 && NPT == 1) || STORE == LBM_STORE_F16S ||
+                                                   STORE == LBM_STORE_BF16S
+                                               ? 768 / THREADS
+                                               : 1)
+    batch_kernel(const BatchEntry* __restrict__ tab, const int* __restrict__ tile_start, int n_inst,
+                 int total_tiles, const int* __restrict__ gbase, int k) {
+  // the current lattice's entry, staged in shared memory: the body reads its
+  // parameters many times per tile, and in global memory the streaming
+  // population traffic would evict them from L1
+  static_assert(sizeof(BatchEntry) % 16 == 0, "entry copied in 16-byte words");
+  __shared__ __align__(16) unsigned char ebuf[sizeof(BatchEntry)];
+  const BatchEntry& e = *reinterpret_cast<const BatchEntry*>(ebuf);
+  int staged = -1;
   const int g = *gbase + k;
-  for (int tile = blockIdx.x; tile < total_tiles; tile += gridDim.x) {
+  const int groups = (total_tiles + kTileGroup - 1) / kTileGroup;
+  for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+    const int t0 = grp * kTileGroup, t1 = min(total_tiles, t0 + kTileGroup);
     int lo = 0, hi = n_inst - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (__ldg(tile_start + mid) <= tile) lo = mid;
+      if (__ldg(tile_start + mid) <= t0) lo = mid;
       else hi = mid - 1;
     }
-    const BatchEntry& e = tab[lo];
-    if (g < e.s0 || g >= e.s_end) continue;
-    const int local = tile - __ldg(tile_start + lo);
-    const int y = local / e.xblocks, xb = local - y * e.xblocks;
-    const bool odd = (g - e.s0) & 1;
-    const void* pin = odd ? e.pop_b : e.pop_a;
-    void* pout = odd ? e.pop_a : e.pop_b;
-    const void* ain = odd ? e.aux_b : e.aux_a;
-    void* aout = odd ? e.aux_a : e.aux_b;
-    const int x0 = (xb * THREADS + threadIdx.x) * NPT;
-    if constexpr (STORE == LBM_STORE_FX64)
-      fused_fx_body<NPT, true, true>(e.P, pin, pout, ain, aout, x0, y);
-    else
-      fused_v2_body<STORE, NPT, true, true>(e.P, pin, pout, ain, aout, x0, y, hash32(e.P.seed + (uint32_t)(g - e.s0)));
+    int next = lo + 1 < n_inst ? __ldg(tile_start + lo + 1) : total_tiles;
+    for (int tile = t0; tile < t1; ++tile) {
+      while (tile >= next) {
+        ++lo;
+        next = lo + 1 < n_inst ? __ldg(tile_start + lo + 1) : total_tiles;
+      }
+      if (lo != staged) {
+        __syncthreads();  // every thread is done with the previous entry
+        const uint4* src = reinterpret_cast<const uint4*>(tab + lo);
+        uint4* dst = reinterpret_cast<uint4*>(ebuf);
+        for (int w = threadIdx.x; w < (int)(sizeof(BatchEntry) / 16); w += THREADS) dst[w] = __ldg(src + w);
+        __syncthreads();
+        staged = lo;
+      }
+      if (g < e.s0 || g >= e.s_end) continue;
+      const int local = tile - __ldg(tile_start + lo);
+      const int y = local / e.xblocks, xb = local - y * e.xblocks;
+      const bool odd = (g - e.s0) & 1;
+      const void* pin = odd ? e.pop_b : e.pop_a;
+      void* pout = odd ? e.pop_a : e.pop_b;
+      const void* ain = odd ? e.aux_b : e.aux_a;
+      void* aout = odd ? e.aux_a : e.aux_b;
+      const int x0 = (xb * THREADS + threadIdx.x) * NPT;
+      if constexpr (STORE == LBM_STORE_FX64)
+        fused_fx_body<NPT, true, true>(e.P, pin, pout, ain, aout, x0, y);
+      else
+        fused_v2_body<STORE, NPT, true, true>(e.P, pin, pout, ain, aout, x0, y, hash32(e.P.seed + (uint32_t)(g - e.s0)));
+    }
   }
 }
 
@@ -129,7 +162,7 @@ static int launch_batch(const void* table, int n, int tiles, int* gbase, int nst
     }
     blocks = fill;
   }
-  blocks = std::min(blocks, std::max(1, tiles));
+  blocks = std::min(blocks, std::max(1, (tiles + kTileGroup - 1) / kTileGroup));
   for (int k = 0; k < nsteps; ++k) {
     batch_kernel<STORE, NPT, THREADS><<<blocks, THREADS, 0, s>>>(tab, start, n, tiles, gbase, k);
     count_launch();

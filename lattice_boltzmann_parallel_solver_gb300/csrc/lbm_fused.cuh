@@ -517,7 +517,7 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
 // when (g - s0) is even.  g = *gbase + k, so a captured graph of launches
 // k = 0..K-1 followed by lbm_batch_advance stays valid across replays.
 // ---------------------------------------------------------------------------
-struct BatchEntry {
+struct __align__(16) BatchEntry {
   KParams P;
   void* pop_a;
   void* pop_b;
