@@ -41,7 +41,7 @@ def parse():
     p.add_argument("--storage", default="fx64", choices=sorted(BYTES_PER_NODE))
     p.add_argument("--exact", action="store_true", help="NumPy-order float64 arithmetic")
     p.add_argument("--no-extras", action="store_true", help="skip variants, e2e, CPU baseline and the other configs")
-    p.add_argument("--workload", default="cavity", choices=["cavity", "shear", "vk", "batch", "serve"],
+    p.add_argument("--workload", default="cavity", choices=["cavity", "shear", "vk", "batch", "serve", "batch_step"],
                    help="cavity: the headline line; the others print one config's results and exit")
     p.add_argument("--configs", default="shear,vk,batch,serve", help="other configs added to the headline line")
     return p.parse_args()
@@ -190,6 +190,24 @@ def bench_batch(P, steps=20000, n=256):
             "candidates": len(tune), "sequential": seq,
             "omega_range": [min(q["omega"] for q in params), max(q["omega"] for q in params)],
             "stability_risk_instances": sum(q["risky"] for q in params)}
+
+
+def batch_step(P, steps=8):
+    """The 256-lattice batch (f16, 2 nodes per thread, 64 threads) set up and
+    advanced a few steps without the autotuner: the case the batch kernel's
+    ncu capture runs."""
+    import torch
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch, Member
+    params = P.scenarios.batch_sweep_params(256)
+    members = []
+    for j, q in enumerate(params):
+        f, rho, u, om, bnd = P.scenarios.von_karman_device(q["nx"], q["ny"], q["plate"], q["re"], seed=j)
+        members.append(Member(q["nx"], q["ny"], om, bnd, steps=2 * steps, f0=f, rho0=rho, u0=u))
+    b = Batch(members, storage="f16", npt=2, threads=64).start()
+    ms = timed_ms(lambda: b.run(steps))
+    torch.cuda.synchronize()
+    return {"workload": "256 von Karman lattices, f16, npt 2, 64 threads, %d steps (no autotuning)" % steps,
+            "nodes": b.nodes, "ms_per_step": ms / steps}
 
 
 def bench_serve(P, n16=200, n64=40):
@@ -376,7 +394,8 @@ def main():
 
     torch.cuda.set_device(local)
     if args.workload != "cavity":
-        fn = {"shear": bench_shear, "vk": bench_vk, "batch": bench_batch, "serve": bench_serve}[args.workload]
+        fn = {"shear": bench_shear, "vk": bench_vk, "batch": bench_batch, "serve": bench_serve,
+              "batch_step": batch_step}[args.workload]
         print(json.dumps(fn(P)), flush=True)
         return
     if world > 1:
