@@ -103,6 +103,26 @@ def save_velocity_frame(path: str, u) -> None:
     write_png(path, colour_frame(torch.linalg.norm(ut, dim=-1)))
 
 
+def npy_bytes(arr: np.ndarray) -> bytes:
+    """The .npy file save_mpiio (parallelization_utils.py:203-253) writes for a
+    2-D array on one rank: format 1.0, the header dict padded with spaces so
+    that magic + length + header end one byte short of a multiple of 16, then a
+    newline, then the C-order data."""
+    arr = np.ascontiguousarray(arr)
+    assert arr.ndim == 2, "save_mpiio writes two-dimensional arrays"
+    magic_str = b"\x93NUMPY\x01\x00"
+    header = str({"descr": np.lib.format.dtype_to_descr(arr.dtype), "fortran_order": False,
+                  "shape": (int(arr.shape[0]), int(arr.shape[1]))})
+    while (len(header) + len(magic_str) + 2) % 16 != 15:
+        header += " "
+    header += "\n"
+    return magic_str + np.int16(len(header)).astype("<i2").tobytes() + header.encode("latin-1") + arr.tobytes()
+
+
 def save_field_npy(path: str, field) -> None:
-    """A 2-D float64 field as a .npy file, the format save_mpiio writes."""
-    np.save(path, np.ascontiguousarray(A.to_device(field).cpu().numpy()))
+    """A 2-D field (device tensor or host array) as the .npy file save_mpiio
+    writes: the same bytes, readable with numpy.load."""
+    if isinstance(field, torch.Tensor):
+        field = field.detach().cpu().numpy()
+    with open(path, "wb") as fh:
+        fh.write(npy_bytes(np.asarray(field)))
