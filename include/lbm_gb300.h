@@ -215,6 +215,7 @@ typedef struct lbm_batch_lattice {
   int32_t* probe_count;
   uint32_t seed;  /* stochastic rounding: random bits from (seed, g - s0, node, direction) */
   int32_t flags;  /* LBM_FLAG_STOCHASTIC */
+  int32_t rows;   /* rows per tile (0 = 1): a tile is `rows` rows of one row segment */
 } lbm_batch_lattice;
 
 size_t lbm_batch_table_bytes(int32_t n);

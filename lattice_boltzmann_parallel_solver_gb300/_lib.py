@@ -55,7 +55,7 @@ class BatchLattice(C.Structure):
     _fields_ = [("g", vp), ("pop_a", vp), ("pop_b", vp), ("aux_a", vp), ("aux_b", vp), ("pitch", i64),
                 ("omega", f64), ("s0", i32), ("s_end", i32), ("probe_x", i32), ("probe_y", i32),
                 ("probe_cap", i32), ("probe_buf", vp), ("probe_count", vp), ("seed", C.c_uint32),
-                ("flags", i32)]
+                ("flags", i32), ("rows", i32)]
 
 # name: (restype, argtypes)
 SIGNATURES = {

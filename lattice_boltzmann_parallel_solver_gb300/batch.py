@@ -55,7 +55,7 @@ class Batch:
     Members can join (``add``) and leave (``remove``) between runs."""
 
     def __init__(self, members=(), storage: str = "f16", npt: int = 0, threads: int = 128, blocks: int = 0,
-                 device: str = "cuda", stochastic: bool = None):
+                 device: str = "cuda", stochastic: bool = None, rows: int = 1):
         A.require_cuda()
         self.stochastic = storage in ("f16", "bf16") if stochastic is None else bool(stochastic)
         self.storage = storage
@@ -64,6 +64,7 @@ class Batch:
         self.npt = npt or {"fx64": 1, "f64": 2}.get(storage, 4)
         self.threads = threads
         self.blocks = blocks
+        self.rows = int(rows)           # rows per tile
         self.gbase = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.g = 0                    # host mirror of the global step
         self.members = []
@@ -144,6 +145,7 @@ class Batch:
                 c.probe_x = c.probe_y = -1
             c.seed = int(m.seed) & 0xFFFFFFFF
             c.flags = _lib.FLAG_STOCHASTIC if self.stochastic else 0
+            c.rows = self.rows
         size = int(_lib.load().lbm_batch_table_bytes(n))
         self.table = torch.empty(size, dtype=torch.uint8, device=self.device)
         tiles = ctypes.c_int32(0)
@@ -229,17 +231,19 @@ class Batch:
 
 
 def autotune(batch: Batch, candidates=None, steps: int = 6, warmup: int = 2):
-    """Pick nodes per thread, threads per block and persistent grid size for a
-    batch by timing each candidate on the batch itself.  Call it before
+    """Pick nodes per thread, threads per block, persistent grid size and rows
+    per tile for a batch by timing each candidate on the batch itself.  Call it before
     ``start()``: the timed steps run on the members' uninitialised buffers
     (probes off) and the global step counter is reset afterwards."""
     sms = torch.cuda.get_device_properties(batch.device).multi_processor_count
     if candidates is None:
         npts = {"fx64": (1, 2), "f16": (2, 4, 8), "bf16": (2, 4, 8)}.get(batch.storage, (2, 4))
-        candidates = [(p, t, b) for p in npts for t in (64, 128, 256) for b in (0, 2 * sms, 8 * sms)]
+        candidates = [(p, t, b, r) for p in npts for t in (64, 128, 256) for b in (0, 8 * sms) for r in (1, 2, 4)]
     best, results = None, []
-    for npt, threads, blocks in candidates:
-        batch.npt, batch.threads, batch.blocks = npt, threads, blocks
+    for cand in candidates:
+        npt, threads, blocks = cand[:3]
+        rows = cand[3] if len(cand) > 3 else 1
+        batch.npt, batch.threads, batch.blocks, batch.rows = npt, threads, blocks, rows
         try:
             batch._build(with_probes=False)
         except (AssertionError, NotImplementedError):
@@ -253,13 +257,13 @@ def autotune(batch: Batch, candidates=None, steps: int = 6, warmup: int = 2):
         e1.record()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1) / steps
-        results.append({"npt": npt, "threads": threads, "blocks": blocks, "ms_per_step": ms,
+        results.append({"npt": npt, "threads": threads, "blocks": blocks, "rows": rows, "ms_per_step": ms,
                         "glups": batch.nodes / (ms * 1e-3) / 1e9})
         if best is None or ms < best[0]:
-            best = (ms, npt, threads, blocks)
+            best = (ms, npt, threads, blocks, rows)
         del t0
     batch.g = 0
     batch.gbase.zero_()
-    _, batch.npt, batch.threads, batch.blocks = best
+    _, batch.npt, batch.threads, batch.blocks, batch.rows = best
     batch.tuning = results
     return results

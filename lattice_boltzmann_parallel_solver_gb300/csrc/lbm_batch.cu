@@ -55,17 +55,21 @@ __global__ void __launch_bounds__(THREADS, (STORE == LBM_STORE_FX64 && NPT == 1)
       }
       if (g < e.s0 || g >= e.s_end) continue;
       const int local = tile - __ldg(tile_start + lo);
-      const int y = local / e.xblocks, xb = local - y * e.xblocks;
+      const int yb = local / e.xblocks, xb = local - yb * e.xblocks;
       const bool odd = (g - e.s0) & 1;
       const void* pin = odd ? e.pop_b : e.pop_a;
       void* pout = odd ? e.pop_a : e.pop_b;
       const void* ain = odd ? e.aux_b : e.aux_a;
       void* aout = odd ? e.aux_a : e.aux_b;
       const int x0 = (xb * THREADS + threadIdx.x) * NPT;
-      if constexpr (STORE == LBM_STORE_FX64)
-        fused_fx_body<NPT, true, true>(e.P, pin, pout, ain, aout, x0, y);
-      else
-        fused_v2_body<STORE, NPT, true, true>(e.P, pin, pout, ain, aout, x0, y, hash32(e.P.seed + (uint32_t)(g - e.s0)));
+      const uint32_t seed = hash32(e.P.seed + (uint32_t)(g - e.s0));
+      const int y1 = min((yb + 1) * e.rows, e.P.g.ny);
+      for (int y = yb * e.rows; y < y1; ++y) {
+        if constexpr (STORE == LBM_STORE_FX64)
+          fused_fx_body<NPT, true, true>(e.P, pin, pout, ain, aout, x0, y);
+        else
+          fused_v2_body<STORE, NPT, true, true>(e.P, pin, pout, ain, aout, x0, y, seed);
+      }
     }
   }
 }
@@ -127,8 +131,9 @@ int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_
     e.s_end = L.s_end;
     const int chunks = (L.g->nx + npt - 1) / npt;
     e.xblocks = (chunks + threads - 1) / threads;
+    e.rows = L.rows > 0 ? L.rows : 1;
     start[(size_t)j] = (int)tiles;
-    tiles += (int64_t)e.xblocks * L.g->ny;
+    tiles += (int64_t)e.xblocks * ((L.g->ny + e.rows - 1) / e.rows);
   }
   if (tiles >= ((int64_t)1 << 31)) return set_error(LBM_ERR_ARG, "too many tiles");
   char* dst = static_cast<char*>(table);

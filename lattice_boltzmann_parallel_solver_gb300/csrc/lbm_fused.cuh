@@ -524,6 +524,7 @@ struct __align__(16) BatchEntry {
   void* aux_a;
   void* aux_b;
   int xblocks;
+  int rows;  // rows per tile
   int s0, s_end;
 };
 

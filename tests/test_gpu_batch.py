@@ -42,12 +42,13 @@ def alone(pkg, m, storage, npt):
     return lat.set_state(m.f0, m.rho0, m.u0).step(m.steps)
 
 
-@pytest.mark.parametrize("storage,npt,threads", [("fx64", 1, 128), ("fx64", 2, 64), ("f64", 2, 128), ("f32", 4, 64), ("f16", 4, 128),
-                                                 ("f16", 8, 256), ("bf16", 2, 128)])
-def test_batch_members_equal_lone_runs(pkg, storage, npt, threads):
+@pytest.mark.parametrize("storage,npt,threads,rows", [("fx64", 1, 128, 1), ("fx64", 2, 64, 3), ("f64", 2, 128, 1),
+                                                      ("f32", 4, 64, 2), ("f16", 4, 128, 1), ("f16", 8, 256, 4),
+                                                      ("bf16", 2, 128, 5)])
+def test_batch_members_equal_lone_runs(pkg, storage, npt, threads, rows):
     from lattice_boltzmann_parallel_solver_gb300.batch import Batch
     ms = members(pkg, steps=(30, 17, 25, 30, 4))
-    b = Batch(ms, storage=storage, npt=npt, threads=threads).start()
+    b = Batch(ms, storage=storage, npt=npt, threads=threads, rows=rows).start()
     b.run()
     for j, m in enumerate(ms):
         got = b.read(j)[0]
