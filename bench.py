@@ -370,6 +370,32 @@ def reference_arm(args):
 
 
 # ---------------------------------------------------------------------------
+# ranks (one replica per GPU under torchrun)
+# ---------------------------------------------------------------------------
+def rank_barrier(world, dist, sync=None):
+    """All ranks meet (when there are several), then the device drains."""
+    if world > 1:
+        dist.barrier()
+    if sync is not None:
+        sync()
+
+
+def slowest_over_ranks(seconds, world, dist, device="cuda"):
+    """The maximum of the ranks' timed spans: the whole job took that long."""
+    if world == 1:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_mlups(world, nodes, steps, seconds):
+    """Lattice updates of all ranks (each runs its own replica) per second, in millions."""
+    return world * nodes * steps / seconds / 1e6
+
+
+# ---------------------------------------------------------------------------
 # GPU arm
 # ---------------------------------------------------------------------------
 def main():
@@ -402,16 +428,10 @@ def main():
         dist.init_process_group("nccl")
 
     def barrier():
-        if world > 1:
-            dist.barrier()
-        torch.cuda.synchronize()
+        rank_barrier(world, dist, torch.cuda.synchronize)
 
     def slowest(seconds):
-        if world == 1:
-            return seconds
-        t = torch.tensor([seconds], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return slowest_over_ranks(seconds, world, dist)
 
     n = args.n
     bnd = cavity_boundary_conditions(n, n, 0.1, 1.0)
@@ -447,7 +467,7 @@ def main():
     algo = BYTES_PER_NODE[args.storage] * nodes
     achieved = algo / per_launch / 1e9
     tpn = profile_traffic_per_node(args.storage)
-    value = world * nodes * args.steps / secs / 1e6
+    value = job_mlups(world, nodes, args.steps, secs)
     del lat
     torch.cuda.empty_cache()
 
