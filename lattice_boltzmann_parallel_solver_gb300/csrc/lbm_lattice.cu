@@ -496,15 +496,17 @@ int lbm_step_f64_host(const lbm_geometry* g, const double* f, const double* rho,
   cuda_ok(cudaStreamWaitEvent(sc, start, 0));
   cuda_ok(cudaStreamWaitEvent(sd, start, 0));
   std::vector<cudaEvent_t> in_ready(K), out_ready(K);
-  for (int k = 0; k < K && st == LBM_OK; ++k) {
+  auto upload = [&](int k) {
+    if (st != LBM_OK) return;
     const int64_t a = xs(k), w = xs(k + 1) - xs(k);
     cuda_ok(cudaMemcpyAsync(fin + 9 * a * ny, f + 9 * a * ny, 9 * w * ny * sizeof(double), cudaMemcpyHostToDevice, sh));
     cuda_ok(cudaMemcpyAsync(rin + a * ny, rho + a * ny, w * ny * sizeof(double), cudaMemcpyHostToDevice, sh));
     cuda_ok(cudaMemcpyAsync(uin + 2 * a * ny, u + 2 * a * ny, 2 * w * ny * sizeof(double), cudaMemcpyHostToDevice, sh));
     in_ready[k] = event();
     cuda_ok(cudaEventRecord(in_ready[k], sh));
-  }
+  };
   auto init = [&](int k) {
+    if (st != LBM_OK) return;
     KParams P = G;
     P.xb = xs(k);
     P.xe = xs(k + 1);
@@ -520,8 +522,8 @@ int lbm_step_f64_host(const lbm_geometry* g, const double* f, const double* rho,
     const int e = exact ? launch<LBM_STORE_F64, true, MODE_INIT>(P, sc) : launch<LBM_STORE_F64, false, MODE_INIT>(P, sc);
     if (e != LBM_OK && st == LBM_OK) st = e;
   };
-  std::vector<int> order;  // slabs in the order they are read out
   auto read = [&](int k) {
+    if (st != LBM_OK) return;
     KParams P = G;
     P.xb = xs(k);
     P.xe = xs(k + 1);
@@ -536,31 +538,45 @@ int lbm_step_f64_host(const lbm_geometry* g, const double* f, const double* rho,
     if (e != LBM_OK && st == LBM_OK) st = e;
     out_ready[k] = event();
     cuda_ok(cudaEventRecord(out_ready[k], sc));
-    order.push_back(k);
   };
-  // Read-out of slab k pulls from columns of slabs k-1 and k+1 (periodic in x),
-  // so it follows their collisions.  The pressure rewrite writes columns 0 and
-  // nx-1 from columns nx-2 and 1: with it, every collision runs first.
-  if (g->pressure || K < 3) {
-    for (int k = 0; k < K; ++k) init(k);
-    for (int k = 0; k < K; ++k) read(k);
-  } else {
-    init(0);
-    init(1);
-    for (int k = 2; k < K; ++k) {
-      init(k);
-      read(k - 1);
-    }
-    read(K - 1);
-    read(0);
-  }
-  for (int k : order) {
-    if (st != LBM_OK) break;
+  auto download = [&](int k) {
+    if (st != LBM_OK) return;
     const int64_t a = xs(k), w = xs(k + 1) - xs(k);
     cuda_ok(cudaStreamWaitEvent(sd, out_ready[k], 0));
     cuda_ok(cudaMemcpyAsync(f_out + 9 * a * ny, fo + 9 * a * ny, 9 * w * ny * sizeof(double), cudaMemcpyDeviceToHost, sd));
     cuda_ok(cudaMemcpyAsync(rho_out + a * ny, ro + a * ny, w * ny * sizeof(double), cudaMemcpyDeviceToHost, sd));
     cuda_ok(cudaMemcpyAsync(u_out + 2 * a * ny, uo + 2 * a * ny, 2 * w * ny * sizeof(double), cudaMemcpyDeviceToHost, sd));
+  };
+  // Read-out of slab k pulls from columns of slabs k-1 and k+1 (periodic in x),
+  // so it follows their collisions.  The pressure rewrite writes columns 0 and
+  // nx-1 from columns nx-2 and 1: with it, every collision runs first.  The
+  // calls are issued interleaved (upload k, collide k, read out and download
+  // k-1), which also keeps the host issuing work while copies from pageable
+  // memory block it.
+  if (g->pressure || K < 3) {
+    for (int k = 0; k < K; ++k) {
+      upload(k);
+      init(k);
+    }
+    for (int k = 0; k < K; ++k) {
+      read(k);
+      download(k);
+    }
+  } else {
+    upload(0);
+    init(0);
+    upload(1);
+    init(1);
+    for (int k = 2; k < K; ++k) {
+      upload(k);
+      init(k);
+      read(k - 1);
+      download(k - 1);
+    }
+    read(K - 1);
+    download(K - 1);
+    read(0);
+    download(0);
   }
   // the caller's stream continues once every copy has landed
   cudaEvent_t done_h = event(), done_c = event(), done_d = event();
