@@ -54,17 +54,20 @@ class Batch:
     """A set of lattices sharing one storage type, advanced in lock step.
     Members can join (``add``) and leave (``remove``) between runs."""
 
-    def __init__(self, members=(), storage: str = "f16", npt: int = 0, threads: int = 128, blocks: int = 0,
-                 device: str = "cuda", stochastic: bool = None, rows: int = 1):
+    def __init__(self, members=(), storage: str = "f16", npt: int = 0, threads: int = 0, blocks: int = 0,
+                 device: str = "cuda", stochastic: bool = None, rows: int = 0):
+        """``npt``, ``threads`` and ``rows`` (nodes per thread, threads per tile,
+        rows per tile) default to what ``autotune`` picks for mixed von Karman
+        batches: 1 x 128 x 4 for fx64, 2 x 64 x 4 for the 16-bit storages."""
         A.require_cuda()
         self.stochastic = storage in ("f16", "bf16") if stochastic is None else bool(stochastic)
         self.storage = storage
         self.store_id, self.pop_dtype, self.aux_dtype = STORAGES[storage]
         self.device = torch.device(device)
-        self.npt = npt or {"fx64": 1, "f64": 2}.get(storage, 4)
-        self.threads = threads
+        self.npt = npt or {"fx64": 1, "f64": 2, "f16": 2, "bf16": 2}.get(storage, 4)
+        self.threads = threads or {"f16": 64, "bf16": 64}.get(storage, 128)
         self.blocks = blocks
-        self.rows = int(rows)           # rows per tile
+        self.rows = int(rows) or 4      # rows per tile
         self.gbase = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.g = 0                    # host mirror of the global step
         self.members = []

@@ -98,7 +98,7 @@ def _row(nx, ny, y):
 class ServingEngine:
     """Admits, batches and retires lattice solves on one GPU."""
 
-    def __init__(self, storage="f16", hbm_budget=64 << 30, max_slots=128, tick_steps=500, npt=0, threads=128,
+    def __init__(self, storage="f16", hbm_budget=64 << 30, max_slots=128, tick_steps=500, npt=0, threads=0,
                  blocks=0, device="cuda"):
         self.storage = storage
         self.hbm_budget = int(hbm_budget)
