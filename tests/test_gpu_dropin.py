@@ -242,3 +242,33 @@ def test_host_buffer_step_matches_device_step(name, slabs):
             ref = O.run(f, rho, u, 1.3, 1, None if name == "none" else O.cavity_boundary(nx, ny, 0.1, 1.0))
             for a, b in zip(got, ref):
                 assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (2, 3), (5, 130), (33, 7), (130, 5)])
+@pytest.mark.parametrize("slabs", [0, 4, 64])
+def test_host_buffer_step_edge_sizes(shape, slabs):
+    """Tiny and ragged lattices, and more slabs than columns: the host-buffer
+    step still equals the device step bit for bit, and the oracle in exact mode."""
+    from lattice_boltzmann_parallel_solver_gb300 import lattice_boltzmann_method as M
+    nx, ny = shape
+    rng = np.random.default_rng(nx * 100 + ny)
+    rho = rng.uniform(0.9, 1.1, shape)
+    u = rng.normal(0, 0.03, shape + (2,))
+    f = O.equilibrium(rho, u) + rng.normal(0, 1e-3, shape + (9,))
+    geo = M.empty_geometry(nx, ny)
+    host = M._step_host(geo, f, rho, u, 1.2, M._lib.FLAG_EXACT, M.A.NUMPY, slabs=slabs)
+    ref = O.run(f, rho, u, 1.2, 1)
+    for a, b in zip(host, ref):
+        assert np.array_equal(a, b)
+
+
+def test_host_buffer_step_rejects_bad_shapes():
+    from lattice_boltzmann_parallel_solver_gb300 import lattice_boltzmann_method as M
+    f = np.ones((4, 5, 8))
+    with pytest.raises(AssertionError):
+        M.lattice_boltzmann_step(f, np.ones((4, 5)), np.zeros((4, 5, 2)), 1.0)
+    f = np.ones((4, 5, 9))
+    with pytest.raises(AssertionError):
+        M.lattice_boltzmann_step(f, np.ones((4, 6)), np.zeros((4, 5, 2)), 1.0)
+    with pytest.raises(AssertionError):
+        M.lattice_boltzmann_step(f, np.ones((4, 5)), np.zeros((4, 5, 2)), 2.5)
