@@ -64,11 +64,16 @@ __global__ void __launch_bounds__(THREADS, (STORE == LBM_STORE_FX64 && NPT == 1)
       const int x0 = (xb * THREADS + threadIdx.x) * NPT;
       const uint32_t seed = hash32(e.P.seed + (uint32_t)(g - e.s0));
       const int y1 = min((yb + 1) * e.rows, e.P.g.ny);
+      // lattices without the pressure rewrite take the body without it
+      const bool pressure = e.P.g.pressure != 0;
       for (int y = yb * e.rows; y < y1; ++y) {
-        if constexpr (STORE == LBM_STORE_FX64)
-          fused_fx_body<NPT, true, true>(e.P, pin, pout, ain, aout, x0, y);
-        else
-          fused_v2_body<STORE, NPT, true, true>(e.P, pin, pout, ain, aout, x0, y, seed);
+        if constexpr (STORE == LBM_STORE_FX64) {
+          if (pressure) fused_fx_body<NPT, true, true>(e.P, pin, pout, ain, aout, x0, y);
+          else fused_fx_body<NPT, true, false>(e.P, pin, pout, ain, aout, x0, y);
+        } else {
+          if (pressure) fused_v2_body<STORE, NPT, true, true>(e.P, pin, pout, ain, aout, x0, y, seed);
+          else fused_v2_body<STORE, NPT, true, false>(e.P, pin, pout, ain, aout, x0, y, seed);
+        }
       }
     }
   }

@@ -123,6 +123,9 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
   auto work_of_f = [&](R fv, int i) -> R { return SH ? (fv - wr<R>(i)) * kS : fv; };
   auto f_of_work = [&](R v, int i) -> R { return SH ? fma(v, R(1) / kS, wr<R>(i)) : v; };
 
+  // the boundary mask word first: its latency overlaps the population loads
+  const bool has_bc = HAS_BC && P.g.bcmask != nullptr;
+  const uint32_t bcword = has_bc ? __ldg(P.g.bcmask + y * P.g.words + (x0 >> 5)) : 0u;
   R f[9][NPT];
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
@@ -159,9 +162,8 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     }
   }
 
-  if (HAS_BC && P.g.bcmask != nullptr) {
-    const uint32_t word = __ldg(P.g.bcmask + y * P.g.words + (x0 >> 5));
-    const uint32_t bits = (word >> (x0 & 31)) & ((NPT >= 32) ? 0xffffffffu : ((1u << NPT) - 1u));
+  if (has_bc) {
+    const uint32_t bits = (bcword >> (x0 & 31)) & ((NPT >= 32) ? 0xffffffffu : ((1u << NPT) - 1u));
     if (bits) {
       const R* aux_in = static_cast<const R*>(aux_in_v);
 #pragma unroll
@@ -351,6 +353,9 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
   const int xp = x0 + NPT >= nx ? 0 : x0 + NPT;
   const T* pin = static_cast<const T*>(pop_in_v);
 
+  // the boundary mask word first: its latency overlaps the population loads
+  const bool has_bc = HAS_BC && P.g.bcmask != nullptr;
+  const uint32_t bcword = has_bc ? __ldg(P.g.bcmask + y * P.g.words + (x0 >> 5)) : 0u;
   T f[9][NPT];
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
@@ -390,9 +395,8 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
     }
   }
 
-  if (HAS_BC && P.g.bcmask != nullptr) {
-    const uint32_t word = __ldg(P.g.bcmask + y * P.g.words + (x0 >> 5));
-    const uint32_t bits = (word >> (x0 & 31)) & ((NPT >= 32) ? 0xffffffffu : ((1u << NPT) - 1u));
+  if (has_bc) {
+    const uint32_t bits = (bcword >> (x0 & 31)) & ((NPT >= 32) ? 0xffffffffu : ((1u << NPT) - 1u));
     if (bits) {
       const T* aux_in = static_cast<const T*>(aux_in_v);
 #pragma unroll
