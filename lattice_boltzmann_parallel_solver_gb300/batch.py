@@ -57,8 +57,10 @@ class Batch:
     def __init__(self, members=(), storage: str = "f16", npt: int = 0, threads: int = 0, blocks: int = 0,
                  device: str = "cuda", stochastic: bool = None, rows: int = 0):
         """``npt``, ``threads`` and ``rows`` (nodes per thread, threads per tile,
-        rows per tile) default to what ``autotune`` picks for mixed von Karman
-        batches: 1 x 128 x 4 for fx64, 2 x 64 x 4 for the 16-bit storages."""
+        rows per tile) default to what ``autotune`` picks for large mixed von
+        Karman batches: 1 x 128 for fx64, 2 x 64 for the 16-bit storages, and
+        4 rows per tile when the batch has enough row segments to keep every
+        SM busy with them (1 otherwise)."""
         A.require_cuda()
         self.stochastic = storage in ("f16", "bf16") if stochastic is None else bool(stochastic)
         self.storage = storage
@@ -67,7 +69,7 @@ class Batch:
         self.npt = npt or {"fx64": 1, "f64": 2, "f16": 2, "bf16": 2}.get(storage, 4)
         self.threads = threads or {"f16": 64, "bf16": 64}.get(storage, 128)
         self.blocks = blocks
-        self.rows = int(rows) or 4      # rows per tile
+        self.rows = int(rows)           # rows per tile (0: chosen from the batch size)
         self.gbase = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.g = 0                    # host mirror of the global step
         self.members = []
@@ -129,8 +131,19 @@ class Batch:
         return sum(t.numel() * t.element_size() for m in self.members for t in m.pop + m.aux)
 
     # -- work table ----------------------------------------------------------------
+    def _rows(self) -> int:
+        """Rows per tile: the given number, else 4 when the batch has at least
+        64 row segments per SM, else 1."""
+        if self.rows > 0:
+            return self.rows
+        seg = self.threads * self.npt
+        segments = sum(-(-m.nx // seg) * m.ny for m in self.members)
+        sms = torch.cuda.get_device_properties(self.device).multi_processor_count
+        return 4 if segments >= 64 * sms else 1
+
     def _build(self, with_probes=True):
         n = len(self.members)
+        rows = self._rows()
         arr = (BatchLatticeC * n)()
         self._keep = []
         for j, m in enumerate(self.members):
@@ -148,7 +161,7 @@ class Batch:
                 c.probe_x = c.probe_y = -1
             c.seed = int(m.seed) & 0xFFFFFFFF
             c.flags = _lib.FLAG_STOCHASTIC if self.stochastic else 0
-            c.rows = self.rows
+            c.rows = rows
         size = int(_lib.load().lbm_batch_table_bytes(n))
         self.table = torch.empty(size, dtype=torch.uint8, device=self.device)
         tiles = ctypes.c_int32(0)

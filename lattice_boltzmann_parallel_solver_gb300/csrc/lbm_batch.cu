@@ -8,9 +8,10 @@
 
 namespace lbm {
 
-// Tiles are handed out in groups of kTileGroup consecutive tiles (mostly of one
-// lattice), so the owner search and the entry's cache lines are shared by the
-// group; groups are strided over the persistent grid.
+// Tiles are handed out in groups of `group` consecutive tiles (mostly of one
+// lattice), so the owner search and the staged entry are shared by the group;
+// groups are strided over the persistent grid.  The launcher makes groups
+// smaller when there are too few tiles to give every block several groups.
 constexpr int kTileGroup = 8;
 
 // registers capped so that 768 threads fit on an SM (the body with every
@@ -21,7 +22,7 @@ __global__ void __launch_bounds__(THREADS, (STORE == LBM_STORE_FX64 && NPT == 1)
                                                ? 768 / THREADS
                                                : 1)
     batch_kernel(const BatchEntry* __restrict__ tab, const int* __restrict__ tile_start, int n_inst,
-                 int total_tiles, const int* __restrict__ gbase, int k) {
+                 int total_tiles, const int* __restrict__ gbase, int k, int group) {
   // the current lattice's entry, staged in shared memory: the body reads its
   // parameters many times per tile, and in global memory the streaming
   // population traffic would evict them from L1
@@ -30,9 +31,9 @@ __global__ void __launch_bounds__(THREADS, (STORE == LBM_STORE_FX64 && NPT == 1)
   const BatchEntry& e = *reinterpret_cast<const BatchEntry*>(ebuf);
   int staged = -1;
   const int g = *gbase + k;
-  const int groups = (total_tiles + kTileGroup - 1) / kTileGroup;
+  const int groups = (total_tiles + group - 1) / group;
   for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
-    const int t0 = grp * kTileGroup, t1 = min(total_tiles, t0 + kTileGroup);
+    const int t0 = grp * group, t1 = min(total_tiles, t0 + group);
     int lo = 0, hi = n_inst - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
@@ -172,9 +173,11 @@ static int launch_batch(const void* table, int n, int tiles, int* gbase, int nst
     }
     blocks = fill;
   }
-  blocks = std::min(blocks, std::max(1, (tiles + kTileGroup - 1) / kTileGroup));
+  // groups of up to kTileGroup tiles, but at least two groups per block
+  const int group = std::max(1, std::min(kTileGroup, tiles / (2 * blocks)));
+  blocks = std::min(blocks, std::max(1, (tiles + group - 1) / group));
   for (int k = 0; k < nsteps; ++k) {
-    batch_kernel<STORE, NPT, THREADS><<<blocks, THREADS, 0, s>>>(tab, start, n, tiles, gbase, k);
+    batch_kernel<STORE, NPT, THREADS><<<blocks, THREADS, 0, s>>>(tab, start, n, tiles, gbase, k, group);
     count_launch();
     if (int e = check_launch("batch_kernel")) return e;
   }

@@ -104,7 +104,9 @@ class ServingEngine:
         self.hbm_budget = int(hbm_budget)
         self.max_slots = max_slots
         self.tick_steps = tick_steps
-        self.batch = Batch([], storage=storage, npt=npt, threads=threads, blocks=blocks, device=device)
+        # one-row tiles: the batch changes every tick, and its tail (the last long
+        # requests) is a handful of lattices that need every tile they can get
+        self.batch = Batch([], storage=storage, npt=npt, threads=threads, blocks=blocks, device=device, rows=1)
         self.live = []          # (Request, Member)
         self.used = 0
         self.stats = {"ticks": 0, "max_live": 0, "steps": 0}
