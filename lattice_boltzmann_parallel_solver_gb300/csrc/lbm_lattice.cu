@@ -178,9 +178,12 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
   }
 }
 
-// the 16-bit storages are issue-bound: registers capped so that 1024 threads fit on an SM
+// the float32 and 16-bit storages: registers capped so that 1024 threads fit on an SM
 template <int STORE, int NPT, int THREADS, bool HAS_BC, bool HAS_PRESSURE>
-__global__ void __launch_bounds__(THREADS, (STORE == LBM_STORE_F16S || STORE == LBM_STORE_BF16S) ? 1024 / THREADS : 1)
+__global__ void __launch_bounds__(THREADS, (STORE == LBM_STORE_F16S || STORE == LBM_STORE_BF16S ||
+                                            (STORE == LBM_STORE_F32 && NPT <= 2))
+                                               ? 1024 / THREADS
+                                               : 1)
     fused_v2_kernel(const __grid_constant__ KParams P) {
   fused_v2_body<STORE, NPT, HAS_BC, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out,
                                                   (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y, P.seed);
@@ -269,7 +272,7 @@ static int default_npt(int storage) {
   switch (storage) {
     case LBM_STORE_F64: return 2;
     case LBM_STORE_FX64: return 1;
-    case LBM_STORE_F32: return 4;
+    case LBM_STORE_F32: return 2;
     default: return 4;
   }
 }
