@@ -75,7 +75,7 @@ def test_resident_f64_exact_and_fast(pkg, name, steps):
 
 
 @pytest.mark.parametrize("storage", ["f64", "fx64"])
-@pytest.mark.parametrize("name", ["shear", "couette", "cavity"])
+@pytest.mark.parametrize("name", ["shear", "couette", "poiseuille", "vk", "cavity"])
 def test_resident_f64_2000_steps(pkg, name, storage):
     nx, ny, om, f, rho, u, obnd, pbnd = scenario(name)
     ref = O.run(f, rho, u, om, 2000, obnd)
