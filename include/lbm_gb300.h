@@ -66,6 +66,12 @@ typedef struct lbm_geometry {
   uint32_t pressure_in_dirs, pressure_out_dirs;
   double rho_in, rho_out;
   int32_t outlet; /* some node uses LBM_SRC_OUTLET */
+  /* device, the n_bcnodes linear indices y*nx + x (ascending) of the nodes with a
+   * bcmask bit.  With it the vectorised step runs its boundary-free body over the
+   * whole lattice and then recomputes just these nodes with their sources; NULL
+   * (or LBM_FLAG_BC_INLINE) applies the sources inside the step. */
+  const int32_t* bcnodes;
+  int32_t n_bcnodes;
 } lbm_geometry;
 
 /* ---- storage / arithmetic of the resident state ------------------------- */
@@ -79,6 +85,7 @@ typedef struct lbm_geometry {
 #define LBM_FLAG_GENERIC 2 /* use the one-node-per-thread kernel instead of the vectorised one */
 #define LBM_FLAG_NPT_SHIFT 4 /* bits 4..7: nodes per thread of the vectorised kernel (0 = default) */
 #define LBM_FLAG_STOCHASTIC 256 /* 16-bit storages: round stored deviations stochastically */
+#define LBM_FLAG_BC_INLINE 1024 /* boundary sources inside the vectorised step even when g->bcnodes is set */
 
 /* ---- library ------------------------------------------------------------ */
 int lbm_version(void);

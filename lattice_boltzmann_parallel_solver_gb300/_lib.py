@@ -26,6 +26,7 @@ FLAG_EXACT = 1
 FLAG_GENERIC = 2
 FLAG_NPT_SHIFT = 4
 FLAG_STOCHASTIC = 256
+FLAG_BC_INLINE = 1024
 
 vp = C.c_void_p
 i32 = C.c_int32
@@ -44,6 +45,7 @@ class Geometry(C.Structure):
         ("pressure_in_dirs", C.c_uint32), ("pressure_out_dirs", C.c_uint32),
         ("rho_in", f64), ("rho_out", f64),
         ("outlet", i32),
+        ("bcnodes", vp), ("n_bcnodes", i32),
     ]
 
 

@@ -23,6 +23,8 @@ struct GeoK {
   int outlet;
   double kconst[LBM_MAX_SETS][9];
   double cconst[LBM_MAX_SETS][9];
+  const int32_t* bcnodes;
+  int n_bcnodes;
 };
 
 struct View {
@@ -131,6 +133,11 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
   for (int i = 0; i < 9; ++i) {
     const int row = cy(i) == 1 ? rm : (cy(i) == -1 ? rp : r0);
     const T* base = pin + i * plane + row;
+    if constexpr (NPT == 1) {
+      // one node per thread (the boundary-node pass): neighbours loaded directly
+      f[i][0] = ld_work(base + (cx(i) == 1 ? xm : (cx(i) == -1 ? xp : x0)), i);
+      continue;
+    }
     T raw[NPT];
     ld_vec<T, NPT>(base + x0, raw);
     R v[NPT];
@@ -228,13 +235,18 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
       pcol = x;
     }
   };
-  if constexpr (SH && NPT % 2 == 0) {
-    // 16-bit storages: two nodes per packed float32 instruction
+  if constexpr (SH) {
+    // 16-bit storages: two nodes per packed float32 instruction (one node per
+    // thread runs the same packed arithmetic on a duplicated pair, so that the
+    // boundary-node pass rounds exactly as the step does)
+    constexpr int K2 = NPT == 1 ? 1 : 2;
+    static_assert(NPT == 1 || NPT % 2 == 0, "packed pairs");
 #pragma unroll
-    for (int k = 0; k < NPT; k += 2) {
+    for (int k = 0; k < NPT; k += K2) {
+      const int k1 = NPT == 1 ? k : k + 1;
       float2 g2[9];
 #pragma unroll
-      for (int i = 0; i < 9; ++i) g2[i] = make_float2(f[i][k], f[i][k + 1]);
+      for (int i = 0; i < 9; ++i) g2[i] = make_float2(f[i][k], f[i][k1]);
       float2 sum, jx, jy;
       moments9x2(g2, sum, jx, jy);
       const float2 rho = add2(f2c(kS), sum);  // s rho
@@ -247,10 +259,10 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
         ga[i] = g2[i].x;
         gb[i] = g2[i].y;
         f[i][k] = ga[i];
-        f[i][k + 1] = gb[i];
+        f[i][k1] = gb[i];
       }
       node_extras(k, sum.x, rho.x, ux.x, uy.x, ga);
-      node_extras(k + 1, sum.y, rho.y, ux.y, uy.y, gb);
+      if (NPT > 1) node_extras(k1, sum.y, rho.y, ux.y, uy.y, gb);
     }
   } else {
 #pragma unroll
@@ -558,6 +570,8 @@ inline bool to_geok(const lbm_geometry* g, GeoK& k) {
   k.outlet = g->outlet;
   std::memcpy(k.kconst, g->kconst, sizeof(k.kconst));
   std::memcpy(k.cconst, g->cconst, sizeof(k.cconst));
+  k.bcnodes = g->n_bcnodes > 0 ? g->bcnodes : nullptr;
+  k.n_bcnodes = k.bcnodes != nullptr ? g->n_bcnodes : 0;
   return true;
 }
 

@@ -196,6 +196,22 @@ __global__ void __launch_bounds__(THREADS, NPT == 1 ? 1024 / THREADS : 1) fused_
                                            (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y);
 }
 
+// The boundary-node pass: after a vectorised step ran its boundary-free body
+// over every node, one thread per listed boundary node recomputes that node
+// with its sources (the same body at one node per thread, so the arithmetic and
+// the random bits are those of the in-step path) and overwrites its outputs.
+template <int STORE, int THREADS, bool HAS_PRESSURE>
+__global__ void __launch_bounds__(THREADS) fixup_v2_kernel(const __grid_constant__ KParams P) {
+  const int t = blockIdx.x * THREADS + threadIdx.x;
+  if (t >= P.g.n_bcnodes) return;
+  const int node = __ldg(P.g.bcnodes + t);
+  const int y = node / P.g.nx, x = node - y * P.g.nx;
+  if constexpr (STORE == LBM_STORE_FX64)
+    fused_fx_body<1, true, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out, x, y);
+  else
+    fused_v2_body<STORE, 1, true, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out, x, y, P.seed);
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -286,8 +302,45 @@ static int v2_npt(int storage, int flags, const KParams& P) {
   return npt;
 }
 
+constexpr int kFixupThreads = 128;
+
+template <int STORE>
+static int launch_fixup(const KParams& P, cudaStream_t s) {
+  const dim3 grid((unsigned)((P.g.n_bcnodes + kFixupThreads - 1) / kFixupThreads));
+  if (P.g.pressure)
+    fixup_v2_kernel<STORE, kFixupThreads, true><<<grid, kFixupThreads, 0, s>>>(P);
+  else
+    fixup_v2_kernel<STORE, kFixupThreads, false><<<grid, kFixupThreads, 0, s>>>(P);
+  count_launch();
+  return check_launch("fixup_v2_kernel");
+}
+
+static int launch_fused_step(int storage, int npt, int flags, const KParams& P, cudaStream_t s);
+
+// One step.  The vectorised kernels run without boundary work when the
+// geometry lists its boundary nodes (and those are at most an eighth of the
+// lattice): the body's boundary block then stays out of the hot loop (it costs
+// registers under the 64-register cap), and the listed nodes are recomputed by
+// the boundary-node pass.
 static int launch_fused(int storage, int flags, const KParams& P, cudaStream_t s) {
   const int npt = v2_npt(storage, flags, P);
+  const bool split = npt > 0 && !(flags & LBM_FLAG_BC_INLINE) && P.g.bcmask != nullptr && P.g.n_bcnodes > 0 &&
+                     (int64_t)P.g.n_bcnodes * 8 <= (int64_t)P.g.nx * P.g.ny;
+  if (!split) return launch_fused_step(storage, npt, flags, P, s);
+  KParams Q = P;
+  Q.g.bcmask = nullptr;
+  if (int e = launch_fused_step(storage, npt, flags, Q, s)) return e;
+  switch (storage) {
+    case LBM_STORE_F64: return launch_fixup<LBM_STORE_F64>(P, s);
+    case LBM_STORE_F32: return launch_fixup<LBM_STORE_F32>(P, s);
+    case LBM_STORE_F16S: return launch_fixup<LBM_STORE_F16S>(P, s);
+    case LBM_STORE_BF16S: return launch_fixup<LBM_STORE_BF16S>(P, s);
+    case LBM_STORE_FX64: return launch_fixup<LBM_STORE_FX64>(P, s);
+    default: return set_error(LBM_ERR_ARG, "unknown storage type");
+  }
+}
+
+static int launch_fused_step(int storage, int npt, int flags, const KParams& P, cudaStream_t s) {
   switch (storage * 16 + npt) {
     case LBM_STORE_F64 * 16 + 2: return launch_v2<LBM_STORE_F64, 2>(P, s);
     case LBM_STORE_F64 * 16 + 4: return launch_v2<LBM_STORE_F64, 4>(P, s);

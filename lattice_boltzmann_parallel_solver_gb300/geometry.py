@@ -79,6 +79,11 @@ class CompiledGeometry:
             self.bcmask = torch.from_numpy(np.ascontiguousarray(bcmask)).to(device)
             g.desc = self.desc.data_ptr()
             g.bcmask = self.bcmask.data_ptr()
+            # linear indices y*nx + x of the boundary nodes, for the boundary-node pass
+            nodes = np.flatnonzero(special.T.reshape(-1)).astype(np.int32)
+            self.bcnodes = torch.from_numpy(nodes).to(device)
+            g.bcnodes = self.bcnodes.data_ptr()
+            g.n_bcnodes = int(nodes.size)
             g.n_kset, g.n_cset = len(ktab), len(ctab)
             for s in range(len(ktab)):
                 for i in range(9):
@@ -87,7 +92,7 @@ class CompiledGeometry:
                 for i in range(9):
                     g.cconst[s][i] = float(ctab[s, i])
         else:
-            self.desc = self.bcmask = None
+            self.desc = self.bcmask = self.bcnodes = None
         if pressure is not None:
             pin, pout, rho_in, rho_out = pressure
             g.pressure = 1
