@@ -317,15 +317,19 @@ static int launch_fixup(const KParams& P, cudaStream_t s) {
 
 static int launch_fused_step(int storage, int npt, int flags, const KParams& P, cudaStream_t s);
 
-// One step.  The vectorised kernels run without boundary work when the
-// geometry lists its boundary nodes (and those are at most an eighth of the
-// lattice): the body's boundary block then stays out of the hot loop (it costs
-// registers under the 64-register cap), and the listed nodes are recomputed by
-// the boundary-node pass.
+// One step.  On lattices of at least kSplitNodes nodes whose geometry lists its
+// boundary nodes (at most an eighth of the lattice), the vectorised kernel runs
+// without boundary work: the body's boundary block then stays out of the hot
+// loop (it costs registers under the 64-register cap), and the listed nodes are
+// recomputed by the boundary-node pass.  Smaller lattices keep one launch per
+// step, whose fixed cost would otherwise double.
+constexpr int64_t kSplitNodes = (int64_t)1 << 20;
+
 static int launch_fused(int storage, int flags, const KParams& P, cudaStream_t s) {
   const int npt = v2_npt(storage, flags, P);
+  const int64_t nodes = (int64_t)P.g.nx * P.g.ny;
   const bool split = npt > 0 && !(flags & LBM_FLAG_BC_INLINE) && P.g.bcmask != nullptr && P.g.n_bcnodes > 0 &&
-                     (int64_t)P.g.n_bcnodes * 8 <= (int64_t)P.g.nx * P.g.ny;
+                     nodes >= kSplitNodes && (int64_t)P.g.n_bcnodes * 8 <= nodes;
   if (!split) return launch_fused_step(storage, npt, flags, P, s);
   KParams Q = P;
   Q.g.bcmask = nullptr;
