@@ -193,9 +193,9 @@ def bench_batch(P, steps=20000, n=256):
 
 
 def batch_step(P, steps=8):
-    """The 256-lattice batch (f16, 2 nodes per thread, 64 threads) set up and
-    advanced a few steps without the autotuner: the case the batch kernel's
-    ncu capture runs."""
+    """The 256-lattice batch (f16, 4 nodes per thread, 64 threads, 2 rows per
+    tile) set up and advanced a few steps without the autotuner: the case the
+    batch kernel's ncu capture runs."""
     import torch
     from lattice_boltzmann_parallel_solver_gb300.batch import Batch, Member
     params = P.scenarios.batch_sweep_params(256)
@@ -203,10 +203,10 @@ def batch_step(P, steps=8):
     for j, q in enumerate(params):
         f, rho, u, om, bnd = P.scenarios.von_karman_device(q["nx"], q["ny"], q["plate"], q["re"], seed=j)
         members.append(Member(q["nx"], q["ny"], om, bnd, steps=2 * steps, f0=f, rho0=rho, u0=u))
-    b = Batch(members, storage="f16", npt=2, threads=64).start()
+    b = Batch(members, storage="f16", npt=4, threads=64, rows=2).start()
     ms = timed_ms(lambda: b.run(steps))
     torch.cuda.synchronize()
-    return {"workload": "256 von Karman lattices, f16, npt 2, 64 threads, %d steps (no autotuning)" % steps,
+    return {"workload": "256 von Karman lattices, f16, npt 4, 64 threads, 2 rows, %d steps (no autotuning)" % steps,
             "nodes": b.nodes, "ms_per_step": ms / steps}
 
 

@@ -221,18 +221,25 @@ typedef struct lbm_batch_lattice {
   double* probe_buf;
   int32_t* probe_count;
   uint32_t seed;  /* stochastic rounding: random bits from (seed, g - s0, node, direction) */
-  int32_t flags;  /* LBM_FLAG_STOCHASTIC */
+  int32_t flags;  /* LBM_FLAG_STOCHASTIC, LBM_FLAG_BC_INLINE */
   int32_t rows;   /* rows per tile (0 = 1): a tile is `rows` rows of one row segment */
 } lbm_batch_lattice;
 
 size_t lbm_batch_table_bytes(int32_t n);
 /* Writes the device work table (table_bytes >= lbm_batch_table_bytes(n)) for
- * tiles of `threads` threads x `npt` nodes; synchronises `stream`. */
+ * tiles of `threads` threads x `npt` nodes; synchronises `stream`.
+ * *bc_chunks receives the boundary-node plan that lbm_batch_run takes: -1 when
+ * the boundary sources run inside the step (some lattice has boundary nodes
+ * but no list of them, or sets LBM_FLAG_BC_INLINE), else the number of
+ * 128-node chunks of listed boundary nodes: each step is then a boundary-free
+ * launch over every node followed by a boundary-node pass over the chunks
+ * (bit-identical results, fewer registers in the hot kernel). */
 int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_t threads, void* table,
-                    size_t table_bytes, int32_t* total_tiles, void* stream);
-/* nsteps batched steps with `blocks` persistent blocks (0 = fill the GPU). */
-int lbm_batch_run(const void* table, int32_t n, int32_t total_tiles, int32_t storage, int32_t npt,
-                  int32_t threads, int32_t* gbase, int32_t nsteps, int32_t blocks, void* stream);
+                    size_t table_bytes, int32_t* total_tiles, int32_t* bc_chunks, void* stream);
+/* nsteps batched steps with `blocks` persistent blocks (0 = fill the GPU);
+ * total_tiles and bc_chunks as lbm_batch_build returned them. */
+int lbm_batch_run(const void* table, int32_t n, int32_t total_tiles, int32_t bc_chunks, int32_t storage,
+                  int32_t npt, int32_t threads, int32_t* gbase, int32_t nsteps, int32_t blocks, void* stream);
 
 #ifdef __cplusplus
 }

@@ -84,8 +84,9 @@ SIGNATURES = {
     "lbm_reduce_scratch_bytes": (C.c_size_t, [i64]),
     "lbm_reduce_moments_f64": (C.c_int, [vp, i64, vp, C.c_size_t, vp, vp]),
     "lbm_batch_table_bytes": (C.c_size_t, [i32]),
-    "lbm_batch_build": (C.c_int, [C.POINTER(BatchLattice), i32, i32, i32, vp, C.c_size_t, C.POINTER(i32), vp]),
-    "lbm_batch_run": (C.c_int, [vp, i32, i32, i32, i32, i32, vp, i32, i32, vp]),
+    "lbm_batch_build": (C.c_int, [C.POINTER(BatchLattice), i32, i32, i32, vp, C.c_size_t, C.POINTER(i32),
+                                  C.POINTER(i32), vp]),
+    "lbm_batch_run": (C.c_int, [vp, i32, i32, i32, i32, i32, i32, vp, i32, i32, vp]),
 }
 
 _lib = None

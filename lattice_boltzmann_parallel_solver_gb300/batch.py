@@ -55,21 +55,26 @@ class Batch:
     Members can join (``add``) and leave (``remove``) between runs."""
 
     def __init__(self, members=(), storage: str = "f16", npt: int = 0, threads: int = 0, blocks: int = 0,
-                 device: str = "cuda", stochastic: bool = None, rows: int = 0):
+                 device: str = "cuda", stochastic: bool = None, rows: int = 0, inline_bc: bool = False):
         """``npt``, ``threads`` and ``rows`` (nodes per thread, threads per tile,
         rows per tile) default to what ``autotune`` picks for large mixed von
-        Karman batches: 1 x 128 for fx64, 2 x 64 for the 16-bit storages, and
-        4 rows per tile when the batch has enough row segments to keep every
-        SM busy with them (1 otherwise)."""
+        Karman batches: 1 x 64 for fx64 with 4 rows, 4 x 64 for the 16-bit
+        storages with 2 rows (rows only when the batch has enough row segments
+        to keep every SM busy with them, 1 otherwise).  Each step is a boundary-free launch
+        over every node followed by a pass over the listed boundary nodes;
+        ``inline_bc`` applies the boundary sources inside the step instead
+        (same results, one launch per step)."""
         A.require_cuda()
         self.stochastic = storage in ("f16", "bf16") if stochastic is None else bool(stochastic)
         self.storage = storage
         self.store_id, self.pop_dtype, self.aux_dtype = STORAGES[storage]
         self.device = torch.device(device)
-        self.npt = npt or {"fx64": 1, "f64": 2, "f16": 2, "bf16": 2}.get(storage, 4)
-        self.threads = threads or {"f16": 64, "bf16": 64}.get(storage, 128)
+        self.npt = npt or {"fx64": 1, "f64": 2}.get(storage, 4)
+        self.threads = threads or {"f16": 64, "bf16": 64, "fx64": 64}.get(storage, 128)
         self.blocks = blocks
         self.rows = int(rows)           # rows per tile (0: chosen from the batch size)
+        self.inline_bc = bool(inline_bc)
+        self.bc_chunks = -1             # boundary-node plan of the work table (-1: sources in the step)
         self.gbase = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.g = 0                    # host mirror of the global step
         self.members = []
@@ -132,14 +137,17 @@ class Batch:
 
     # -- work table ----------------------------------------------------------------
     def _rows(self) -> int:
-        """Rows per tile: the given number, else 4 when the batch has at least
-        64 row segments per SM, else 1."""
+        """Rows per tile: the given number, else (when the batch has at least 64
+        row segments per SM) 2 for the 16-bit storages and 4 for the others,
+        else 1."""
         if self.rows > 0:
             return self.rows
         seg = self.threads * self.npt
         segments = sum(-(-m.nx // seg) * m.ny for m in self.members)
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
-        return 4 if segments >= 64 * sms else 1
+        if segments < 64 * sms:
+            return 1
+        return 2 if self.storage in ("f16", "bf16") else 4
 
     def _build(self, with_probes=True):
         n = len(self.members)
@@ -160,14 +168,15 @@ class Batch:
             else:
                 c.probe_x = c.probe_y = -1
             c.seed = int(m.seed) & 0xFFFFFFFF
-            c.flags = _lib.FLAG_STOCHASTIC if self.stochastic else 0
+            c.flags = (_lib.FLAG_STOCHASTIC if self.stochastic else 0) | \
+                (_lib.FLAG_BC_INLINE if self.inline_bc else 0)
             c.rows = rows
         size = int(_lib.load().lbm_batch_table_bytes(n))
         self.table = torch.empty(size, dtype=torch.uint8, device=self.device)
-        tiles = ctypes.c_int32(0)
+        tiles, chunks = ctypes.c_int32(0), ctypes.c_int32(0)
         _lib.call("lbm_batch_build", arr, n, self.npt, self.threads, self.table.data_ptr(), size,
-                  ctypes.byref(tiles), A.stream())
-        self.tiles = tiles.value
+                  ctypes.byref(tiles), ctypes.byref(chunks), A.stream())
+        self.tiles, self.bc_chunks = tiles.value, chunks.value
         self._graphs.clear()
         self._dirty = False
 
@@ -189,8 +198,8 @@ class Batch:
         if self._dirty and self.members:
             self._build()
         if n > 0 and self.members:
-            _lib.call("lbm_batch_run", self.table.data_ptr(), len(self.members), self.tiles, self.store_id,
-                      self.npt, self.threads, self.gbase.data_ptr(), n, self.blocks, A.stream())
+            _lib.call("lbm_batch_run", self.table.data_ptr(), len(self.members), self.tiles, self.bc_chunks,
+                      self.store_id, self.npt, self.threads, self.gbase.data_ptr(), n, self.blocks, A.stream())
             self.g += n
         return self
 
@@ -204,16 +213,16 @@ class Batch:
             g = self._graphs.get(chunk)
             if g is None:
                 # a zero-step call outside capture settles the default grid size
-                _lib.call("lbm_batch_run", self.table.data_ptr(), len(self.members), self.tiles, self.store_id,
-                          self.npt, self.threads, self.gbase.data_ptr(), 0, self.blocks, A.stream())
+                _lib.call("lbm_batch_run", self.table.data_ptr(), len(self.members), self.tiles, self.bc_chunks,
+                          self.store_id, self.npt, self.threads, self.gbase.data_ptr(), 0, self.blocks, A.stream())
                 g = torch.cuda.CUDAGraph()
                 side = torch.cuda.Stream()
                 side.wait_stream(torch.cuda.current_stream())
                 with torch.cuda.stream(side):
                     with torch.cuda.graph(g, stream=side):
                         _lib.call("lbm_batch_run", self.table.data_ptr(), len(self.members), self.tiles,
-                                  self.store_id, self.npt, self.threads, self.gbase.data_ptr(), chunk, self.blocks,
-                                  side.cuda_stream)
+                                  self.bc_chunks, self.store_id, self.npt, self.threads, self.gbase.data_ptr(),
+                                  chunk, self.blocks, side.cuda_stream)
                 torch.cuda.current_stream().wait_stream(side)
                 self._graphs[chunk] = g
             for _ in range(full):

@@ -1,0 +1,250 @@
+// lbm_batch.cuh -- the batched step kernels and their launcher (many lattices
+// of different sizes advanced by one launch per time step).  Two translation
+// units instantiate the launcher: lbm_batch_inline.cu (boundary sources inside
+// the step) and lbm_batch_split.cu (boundary-free step + boundary-node pass).
+#pragma once
+#include <algorithm>
+#include <cstddef>
+
+#include "lbm_fused.cuh"
+
+namespace lbm {
+
+// Tiles are handed out in groups of `group` consecutive tiles (mostly of one
+// lattice), so the owner search and the staged entry are shared by the group;
+// groups are strided over the persistent grid.  The launcher makes groups
+// smaller when there are too few tiles to give every block several groups.
+constexpr int kTileGroup = 8;
+
+// Registers: the boundary-free body (HAS_BC false, boundary nodes left to
+// batch_fixup_kernel) is capped like the single-lattice kernels, 1024 threads
+// per SM; the body with every boundary form compiled in needs more, 768.
+template <int STORE, int NPT, int THREADS, bool HAS_BC>
+constexpr int batch_min_blocks() {
+  if constexpr ((STORE == LBM_STORE_FX64 && NPT == 1) || STORE == LBM_STORE_F16S || STORE == LBM_STORE_BF16S)
+    return (HAS_BC ? 768 : 1024) / THREADS;
+  else if constexpr (!HAS_BC && STORE == LBM_STORE_F32 && NPT <= 2)
+    return 1024 / THREADS;
+  else
+    return 1;
+}
+
+// The entry's boundary constant tables (kconst, cconst: 2.3 KB of its 2.7 KB)
+// are read only by the boundary sources; a body without them stages the 16-byte
+// words before and after the tables.
+constexpr int kEntryWords = (int)(sizeof(BatchEntry) / 16);
+constexpr int kTablesFirst = (int)((offsetof(BatchEntry, P.g.kconst) + 15) / 16);  // first word inside the tables
+constexpr int kTablesEnd = (int)(offsetof(BatchEntry, P.g.bcnodes) / 16);         // first word holding bytes after them
+static_assert(offsetof(BatchEntry, P.g.cconst) == offsetof(BatchEntry, P.g.kconst) + sizeof(GeoK::kconst) &&
+                  offsetof(BatchEntry, P.g.bcnodes) == offsetof(BatchEntry, P.g.cconst) + sizeof(GeoK::cconst),
+              "the constant tables are contiguous, followed by bcnodes");
+
+// stages lattice `lo`'s entry in the block's shared buffer (every thread of the
+// block calls it with the same `lo`); TABLES: with the boundary constant tables
+template <int THREADS, bool TABLES>
+__device__ __forceinline__ void stage_entry(const BatchEntry* __restrict__ tab, int lo, unsigned char* ebuf) {
+  static_assert(sizeof(BatchEntry) % 16 == 0, "entry copied in 16-byte words");
+  __syncthreads();  // every thread is done with the previous entry
+  const uint4* src = reinterpret_cast<const uint4*>(tab + lo);
+  uint4* dst = reinterpret_cast<uint4*>(ebuf);
+  constexpr int skip = TABLES ? 0 : kTablesEnd - kTablesFirst;
+  for (int w = threadIdx.x; w < kEntryWords - skip; w += THREADS) {
+    const int v = TABLES || w < kTablesFirst ? w : w + skip;
+    dst[v] = __ldg(src + v);
+  }
+  __syncthreads();
+}
+
+// last index j in [0, n) with start[j] <= t (start ascending, start[0] == 0)
+__device__ __forceinline__ int owner_of(const int* __restrict__ start, int n, int t) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(start + mid) <= t) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+template <int STORE, int NPT, int THREADS, bool HAS_BC>
+__global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS, HAS_BC>())
+    batch_kernel(const BatchEntry* __restrict__ tab, const int* __restrict__ tile_start, int n_inst,
+                 int total_tiles, const int* __restrict__ gbase, int k, int group) {
+  // the current lattice's entry, staged in shared memory: the body reads its
+  // parameters many times per tile, and in global memory the streaming
+  // population traffic would evict them from L1
+  __shared__ __align__(16) unsigned char ebuf[sizeof(BatchEntry)];
+  const BatchEntry& e = *reinterpret_cast<const BatchEntry*>(ebuf);
+  int staged = -1;
+  const int g = *gbase + k;
+  const int groups = (total_tiles + group - 1) / group;
+  for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
+    const int t0 = grp * group, t1 = min(total_tiles, t0 + group);
+    int lo = owner_of(tile_start, n_inst, t0);
+    int next = lo + 1 < n_inst ? __ldg(tile_start + lo + 1) : total_tiles;
+    for (int tile = t0; tile < t1; ++tile) {
+      while (tile >= next) {
+        ++lo;
+        next = lo + 1 < n_inst ? __ldg(tile_start + lo + 1) : total_tiles;
+      }
+      if (lo != staged) {
+        stage_entry<THREADS, HAS_BC>(tab, lo, ebuf);
+        staged = lo;
+      }
+      if (g < e.s0 || g >= e.s_end) continue;
+      const int local = tile - __ldg(tile_start + lo);
+      const int yb = local / e.xblocks, xb = local - yb * e.xblocks;
+      const bool odd = (g - e.s0) & 1;
+      const void* pin = odd ? e.pop_b : e.pop_a;
+      void* pout = odd ? e.pop_a : e.pop_b;
+      const void* ain = odd ? e.aux_b : e.aux_a;
+      void* aout = odd ? e.aux_a : e.aux_b;
+      const int x0 = (xb * THREADS + threadIdx.x) * NPT;
+      const uint32_t seed = hash32(e.P.seed + (uint32_t)(g - e.s0));
+      const int y1 = min((yb + 1) * e.rows, e.P.g.ny);
+      // with the sources inside the step, lattices without the pressure rewrite
+      // take the body without it; the boundary-free body leaves the rewrite to
+      // the boundary-node pass
+      const bool pressure = HAS_BC && e.P.g.pressure != 0;
+      for (int y = yb * e.rows; y < y1; ++y) {
+        if constexpr (STORE == LBM_STORE_FX64) {
+          if (pressure) fused_fx_body<NPT, HAS_BC, HAS_BC>(e.P, pin, pout, ain, aout, x0, y);
+          else fused_fx_body<NPT, HAS_BC, false>(e.P, pin, pout, ain, aout, x0, y);
+        } else {
+          if (pressure) fused_v2_body<STORE, NPT, HAS_BC, HAS_BC>(e.P, pin, pout, ain, aout, x0, y, seed);
+          else fused_v2_body<STORE, NPT, HAS_BC, false>(e.P, pin, pout, ain, aout, x0, y, seed);
+        }
+      }
+    }
+  }
+}
+
+// The batched boundary-node pass: after batch_kernel<..., false> stepped every
+// node of every live lattice without boundary sources or pressure rewrite, one
+// thread per pass node recomputes that node with them and overwrites its
+// outputs (the body at one node per thread, the same arithmetic and random
+// bits as the in-step sources).  A lattice's pass nodes are its listed boundary
+// nodes, then, under the pressure rewrite, columns 1 and nx-2 of every row
+// (those not listed already), whose nodes write the rewritten populations of
+// columns nx-1 and 0.  Block b takes chunk b of the chunk list: lattice j owns
+// chunks [bc_start[j], bc_start[j + 1]) of kFixupChunk pass nodes.
+constexpr int kFixupChunk = 128;
+
+inline int64_t pass_nodes(const GeoK& g) {
+  return (g.bcmask != nullptr ? (int64_t)g.n_bcnodes : 0) + (g.pressure ? 2 * (int64_t)g.ny : 0);
+}
+
+template <int STORE>
+__global__ void __launch_bounds__(kFixupChunk)
+    batch_fixup_kernel(const BatchEntry* __restrict__ tab, const int* __restrict__ bc_start, int n_inst,
+                       const int* __restrict__ gbase, int k) {
+  __shared__ __align__(16) unsigned char ebuf[sizeof(BatchEntry)];
+  const BatchEntry& e = *reinterpret_cast<const BatchEntry*>(ebuf);
+  const int g = *gbase + k;
+  const int j = owner_of(bc_start, n_inst, (int)blockIdx.x);
+  stage_entry<kFixupChunk, true>(tab, j, ebuf);
+  if (g < e.s0 || g >= e.s_end) return;
+  const int t = ((int)blockIdx.x - __ldg(bc_start + j)) * kFixupChunk + (int)threadIdx.x;
+  const int nx = e.P.g.nx;
+  const int listed = e.P.g.bcmask != nullptr ? e.P.g.n_bcnodes : 0;
+  int x, y;
+  if (t < listed) {
+    const int node = __ldg(e.P.g.bcnodes + t);
+    y = node / nx;
+    x = node - y * nx;
+  } else {
+    // a pressure column node: (1, y) for even q, (nx-2, y) for odd q
+    const int q = t - listed;
+    if (!e.P.g.pressure || q >= 2 * e.P.g.ny) return;
+    y = q >> 1;
+    x = (q & 1) ? nx - 2 : 1;
+    if ((q & 1) && nx - 2 == 1) return;  // one column: its even entry covers it
+    if (e.P.g.bcmask != nullptr && ((__ldg(e.P.g.bcmask + y * e.P.g.words + (x >> 5)) >> (x & 31)) & 1u))
+      return;  // listed already
+  }
+  const bool odd = (g - e.s0) & 1;
+  const void* pin = odd ? e.pop_b : e.pop_a;
+  void* pout = odd ? e.pop_a : e.pop_b;
+  const void* ain = odd ? e.aux_b : e.aux_a;
+  void* aout = odd ? e.aux_a : e.aux_b;
+  if constexpr (STORE == LBM_STORE_FX64) {
+    if (e.P.g.pressure) fused_fx_body<1, true, true>(e.P, pin, pout, ain, aout, x, y);
+    else fused_fx_body<1, true, false>(e.P, pin, pout, ain, aout, x, y);
+  } else {
+    const uint32_t seed = hash32(e.P.seed + (uint32_t)(g - e.s0));
+    if (e.P.g.pressure) fused_v2_body<STORE, 1, true, true>(e.P, pin, pout, ain, aout, x, y, seed);
+    else fused_v2_body<STORE, 1, true, false>(e.P, pin, pout, ain, aout, x, y, seed);
+  }
+}
+
+// one copy per translation unit (each unit launches its own)
+static __global__ void batch_advance_kernel(int* gbase, int k) { *gbase += k; }
+
+
+template <int STORE, int NPT, int THREADS, bool HAS_BC>
+inline int launch_batch(const void* table, int n, int tiles, int bc_chunks, int* gbase, int nsteps, int blocks,
+                        cudaStream_t s) {
+  const BatchEntry* tab = static_cast<const BatchEntry*>(table);
+  const int* start = reinterpret_cast<const int*>(static_cast<const char*>(table) + (size_t)n * sizeof(BatchEntry));
+  const int* bc_start = start + n;
+  if (blocks <= 0) {
+    // resident blocks of this kernel on the whole GPU, queried on the first
+    // call (make that call outside stream capture) and reused afterwards
+    static int fill = 0;
+    if (fill == 0) {
+      int per_sm = 0, sms = 0, dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<STORE, NPT, THREADS, HAS_BC>, THREADS, 0);
+      fill = std::max(1, sms * std::max(1, per_sm));
+    }
+    blocks = fill;
+  }
+  // groups of up to kTileGroup tiles, but at least two groups per block
+  const int group = std::max(1, std::min(kTileGroup, tiles / (2 * blocks)));
+  blocks = std::min(blocks, std::max(1, (tiles + group - 1) / group));
+  for (int k = 0; k < nsteps; ++k) {
+    batch_kernel<STORE, NPT, THREADS, HAS_BC><<<blocks, THREADS, 0, s>>>(tab, start, n, tiles, gbase, k, group);
+    count_launch();
+    if (int e = check_launch("batch_kernel")) return e;
+    if (!HAS_BC && bc_chunks > 0) {
+      batch_fixup_kernel<STORE><<<bc_chunks, kFixupChunk, 0, s>>>(tab, bc_start, n, gbase, k);
+      count_launch();
+      if (int e = check_launch("batch_fixup_kernel")) return e;
+    }
+  }
+  batch_advance_kernel<<<1, 1, 0, s>>>(gbase, nsteps);
+  count_launch();
+  return check_launch("batch_advance_kernel");
+}
+
+
+// dispatch over (storage, npt, threads) to launch_batch<..., HAS_BC>
+int batch_launch_inline(const void* table, int n, int tiles, int bc_chunks, int storage, int npt, int threads,
+                        int* gbase, int nsteps, int blocks, cudaStream_t s);
+int batch_launch_split(const void* table, int n, int tiles, int bc_chunks, int storage, int npt, int threads,
+                       int* gbase, int nsteps, int blocks, cudaStream_t s);
+
+#define LBM_BATCH_DISPATCH(HAS_BC)                                                                           \
+  do {                                                                                                       \
+    LBM_BATCH_NPT(LBM_STORE_F64, 2, HAS_BC)                                                                  \
+    LBM_BATCH_NPT(LBM_STORE_F64, 4, HAS_BC)                                                                  \
+    LBM_BATCH_NPT(LBM_STORE_FX64, 1, HAS_BC)                                                                 \
+    LBM_BATCH_NPT(LBM_STORE_FX64, 2, HAS_BC)                                                                 \
+    LBM_BATCH_NPT(LBM_STORE_F32, 2, HAS_BC)                                                                  \
+    LBM_BATCH_NPT(LBM_STORE_F32, 4, HAS_BC)                                                                  \
+    LBM_BATCH_NPT(LBM_STORE_F16S, 2, HAS_BC)                                                                 \
+    LBM_BATCH_NPT(LBM_STORE_F16S, 4, HAS_BC)                                                                 \
+    LBM_BATCH_NPT(LBM_STORE_F16S, 8, HAS_BC)                                                                 \
+    LBM_BATCH_NPT(LBM_STORE_BF16S, 2, HAS_BC)                                                                \
+    LBM_BATCH_NPT(LBM_STORE_BF16S, 4, HAS_BC)                                                                \
+    LBM_BATCH_NPT(LBM_STORE_BF16S, 8, HAS_BC)                                                                \
+    return set_error(LBM_ERR_UNSUPPORTED, "no batched kernel for this storage / npt / threads");              \
+  } while (0)
+#define LBM_BATCH_CASE(ST, NP, TH, HAS_BC)               \
+  if (storage == ST && npt == NP && threads == TH)       \
+    return launch_batch<ST, NP, TH, HAS_BC>(table, n, tiles, bc_chunks, gbase, nsteps, blocks, s);
+#define LBM_BATCH_NPT(ST, NP, HAS_BC) \
+  LBM_BATCH_CASE(ST, NP, 64, HAS_BC) LBM_BATCH_CASE(ST, NP, 128, HAS_BC) LBM_BATCH_CASE(ST, NP, 256, HAS_BC)
+
+}  // namespace lbm

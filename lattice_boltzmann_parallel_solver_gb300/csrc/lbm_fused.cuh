@@ -62,9 +62,15 @@ struct KParams {
   fx::QConsts qc;
 };
 
+// skip_bc: a body without its boundary block leaves the probe of a node that
+// the batched boundary-node pass recomputes (a listed boundary node or, under
+// the pressure rewrite, a node of column 1 or nx-2) to that pass
 template <typename R>
-__device__ __forceinline__ void write_probe(const KParams& P, int x, int y, R ux, R uy) {
+__device__ __forceinline__ void write_probe(const KParams& P, int x, int y, R ux, R uy, bool skip_bc = false) {
   if (P.probe_buf != nullptr && x == P.probe_x && y == P.probe_y) {
+    if (skip_bc && ((P.g.pressure && (x == 1 || x == P.g.nx - 2)) ||
+                    (P.g.bcmask != nullptr && ((__ldg(P.g.bcmask + y * P.g.words + (x >> 5)) >> (x & 31)) & 1u))))
+      return;
     const int t = *P.probe_count;
     if (t < P.probe_cap) {
       P.probe_buf[2 * t] = (double)ux;
@@ -224,7 +230,7 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
         up[0] = (double)ux;
         up[P.u_out.sc] = (double)uy;
       }
-      write_probe(P, x, y, ux, uy);
+      write_probe(P, x, y, ux, uy, !HAS_BC);
     }
     if (HAS_PRESSURE && P.g.pressure && k < nvalid && (x == nx - 2 || x == 1)) {
       R br[9];
@@ -472,7 +478,7 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
           up[0] = ux;
           up[P.u_out.sc] = uy;
         }
-        write_probe(P, x, y, ux, uy);
+        write_probe(P, x, y, ux, uy, !HAS_BC);
       }
     }
     if (!fx::collide_q(g, P.qc)) {

@@ -103,3 +103,32 @@ def test_autotune_picks_a_working_config(pkg):
     for j, m in enumerate(ms):
         ref = alone(pkg, m, "f16", b.npt).read()[0]
         assert float((b.read(j)[0] - ref).abs().max()) <= 1e-6
+
+
+@pytest.mark.parametrize("storage", ["fx64", "f64", "f32", "f16", "bf16"])
+def test_boundary_node_pass_equals_inline_sources(pkg, storage):
+    """The default batched step (a boundary-free launch, then the pass over the
+    listed boundary nodes) gives bit-identical states and probe traces to the
+    step with the boundary sources inside it, for walls, the moving lid, the
+    pressure rewrite, inlet/outlet and the plate; the probes sit on a lid node,
+    an inlet node and a pressure-column node, which the pass records."""
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch
+    npt = {"fx64": 1, "f64": 2, "f32": 2}.get(storage, 4)
+    runs = []
+    for inline in (True, False):
+        ms = members(pkg, steps=(40, 33, 40, 40, 40))
+        ms[1].probe = (0, 20)
+        ms[2].probe = (18, 36)
+        ms[3].probe = (48, 9)
+        b = Batch(ms, storage=storage, npt=npt, threads=64, rows=2, inline_bc=inline).start()
+        assert (b.bc_chunks == -1) == inline and (inline or b.bc_chunks > 0)
+        b.run()
+        runs.append((b, ms))
+    (a, _), (b, ms) = runs
+    for j, m in enumerate(ms):
+        fa, ra, ua = a.read(j)
+        fb, rb, ub = b.read(j)
+        assert torch.equal(fa, fb) and torch.equal(ua, ub), (storage, j)
+        if m.probe is not None:
+            ta, tb = a.probe_trace(j), b.probe_trace(j)
+            assert ta.shape[0] == m.steps - 1 and torch.equal(ta, tb), (storage, j)
