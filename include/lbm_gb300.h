@@ -236,7 +236,8 @@ size_t lbm_batch_table_bytes(int32_t n);
  * (bit-identical results, fewer registers in the hot kernel). */
 int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_t threads, void* table,
                     size_t table_bytes, int32_t* total_tiles, int32_t* bc_chunks, void* stream);
-/* nsteps batched steps with `blocks` persistent blocks (0 = fill the GPU);
+/* nsteps batched steps with `blocks` persistent blocks (0 = fill the GPU; more
+ * than half the tile count = one tile per block, a plain grid);
  * total_tiles and bc_chunks as lbm_batch_build returned them. */
 int lbm_batch_run(const void* table, int32_t n, int32_t total_tiles, int32_t bc_chunks, int32_t storage,
                   int32_t npt, int32_t threads, int32_t* gbase, int32_t nsteps, int32_t blocks, void* stream);

@@ -255,15 +255,22 @@ class Batch:
         return m.probe_buf[: 2 * n].view(n, 2)
 
 
+# a grid size above half the tile count gives one tile per block: a plain
+# (non-persistent) grid walked by the hardware block scheduler
+ONE_TILE_PER_BLOCK = 1 << 24
+
+
 def autotune(batch: Batch, candidates=None, steps: int = 6, warmup: int = 2):
-    """Pick nodes per thread, threads per block, persistent grid size and rows
-    per tile for a batch by timing each candidate on the batch itself.  Call it before
+    """Pick nodes per thread, threads per block, grid size (0: one persistent
+    block per resident slot; ONE_TILE_PER_BLOCK) and rows per tile for a
+    batch by timing each candidate on the batch itself.  Call it before
     ``start()``: the timed steps run on the members' uninitialised buffers
     (probes off) and the global step counter is reset afterwards."""
     sms = torch.cuda.get_device_properties(batch.device).multi_processor_count
     if candidates is None:
         npts = {"fx64": (1, 2), "f16": (2, 4, 8), "bf16": (2, 4, 8)}.get(batch.storage, (2, 4))
-        candidates = [(p, t, b, r) for p in npts for t in (64, 128, 256) for b in (0, 8 * sms) for r in (1, 2, 4)]
+        candidates = [(p, t, b, r) for p in npts for t in (64, 128, 256) for b in (0, 8 * sms, ONE_TILE_PER_BLOCK)
+                      for r in (1, 2, 4)]
     best, results = None, []
     for cand in candidates:
         npt, threads, blocks = cand[:3]

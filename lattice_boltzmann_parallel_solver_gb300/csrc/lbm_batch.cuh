@@ -16,12 +16,17 @@ namespace lbm {
 // smaller when there are too few tiles to give every block several groups.
 constexpr int kTileGroup = 8;
 
-// Registers: the boundary-free body (HAS_BC false, boundary nodes left to
-// batch_fixup_kernel) is capped like the single-lattice kernels, 1024 threads
-// per SM; the body with every boundary form compiled in needs more, 768.
+// Registers (measured on the 256-lattice sweep): the 16-bit bodies run fastest
+// at 768 threads per SM (up to 85 registers: no spills at 4 nodes per thread;
+// the loop state that the persistent grid keeps across the body spills under a
+// 64-register cap, 92 against 106 GLUPS); the boundary-free fixed-point body at
+// 1024 threads, as in the single-lattice kernel; with every boundary form
+// compiled in, 768.
 template <int STORE, int NPT, int THREADS, bool HAS_BC>
 constexpr int batch_min_blocks() {
-  if constexpr ((STORE == LBM_STORE_FX64 && NPT == 1) || STORE == LBM_STORE_F16S || STORE == LBM_STORE_BF16S)
+  if constexpr (STORE == LBM_STORE_F16S || STORE == LBM_STORE_BF16S)
+    return 768 / THREADS;
+  else if constexpr (STORE == LBM_STORE_FX64 && NPT == 1)
     return (HAS_BC ? 768 : 1024) / THREADS;
   else if constexpr (!HAS_BC && STORE == LBM_STORE_F32 && NPT <= 2)
     return 1024 / THREADS;
@@ -201,7 +206,7 @@ inline int launch_batch(const void* table, int n, int tiles, int bc_chunks, int*
     blocks = fill;
   }
   // groups of up to kTileGroup tiles, but at least two groups per block
-  const int group = std::max(1, std::min(kTileGroup, tiles / (2 * blocks)));
+  const int group = (int)std::max<int64_t>(1, std::min<int64_t>(kTileGroup, (int64_t)tiles / (2 * (int64_t)blocks)));
   blocks = std::min(blocks, std::max(1, (tiles + group - 1) / group));
   for (int k = 0; k < nsteps; ++k) {
     batch_kernel<STORE, NPT, THREADS, HAS_BC><<<blocks, THREADS, 0, s>>>(tab, start, n, tiles, gbase, k, group);
