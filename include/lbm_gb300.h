@@ -198,8 +198,9 @@ int lbm_reduce_moments_f64(const double* f, int64_t n_nodes, void* scratch, size
 
 /* ---- batched lattices ----------------------------------------------------------- */
 /* Many lattices of different sizes, one storage type, advanced together: one
- * launch per time step covers every live lattice (a flat list of row-segment
- * tiles walked by a persistent grid).  Lattice j is live for global steps
+ * launch per time step covers every live lattice (a flat list of tiles of
+ * consecutive node chunks walked by a grid), followed by the boundary-node
+ * pass (lbm_batch_build).  Lattice j is live for global steps
  * [s0, s_end); at global step g it reads pop_a when (g - s0) is even.  The
  * global step is *gbase (device int) plus the launch's index, and
  * lbm_batch_run ends with a kernel adding nsteps to *gbase, so a captured
@@ -222,12 +223,13 @@ typedef struct lbm_batch_lattice {
   int32_t* probe_count;
   uint32_t seed;  /* stochastic rounding: random bits from (seed, g - s0, node, direction) */
   int32_t flags;  /* LBM_FLAG_STOCHASTIC, LBM_FLAG_BC_INLINE */
-  int32_t rows;   /* rows per tile (0 = 1): a tile is `rows` rows of one row segment */
+  int32_t rows;   /* runs per tile (0 = 1): a tile is `rows` runs of `threads` consecutive chunks of `npt`
+                   nodes, chunks numbered row by row (a run may cross a row end) */
 } lbm_batch_lattice;
 
 size_t lbm_batch_table_bytes(int32_t n);
 /* Writes the device work table (table_bytes >= lbm_batch_table_bytes(n)) for
- * tiles of `threads` threads x `npt` nodes; synchronises `stream`.
+ * tiles of `rows` runs of `threads` threads x `npt` nodes; synchronises `stream`.
  * *bc_chunks receives the boundary-node plan that lbm_batch_run takes: -1 when
  * the boundary sources run inside the step (some lattice has boundary nodes
  * but no list of them, or sets LBM_FLAG_BC_INLINE), else the number of

@@ -1,6 +1,7 @@
-"""Many lattices of different sizes advanced together: one kernel launch per
-time step covers every live lattice (a flat list of row-segment tiles walked
-by a persistent grid), optionally replayed from a captured CUDA graph.
+"""Many lattices of different sizes advanced together: one boundary-free
+launch per time step covers every live lattice (a flat list of tiles of
+consecutive node chunks walked by a grid), a second one the boundary nodes,
+optionally replayed from a captured CUDA graph.
 
 This runs what the reference does one driver loop at a time - for example
 the Reynolds / blockage / width sweeps of ``x_strouhal``
@@ -57,10 +58,10 @@ class Batch:
     def __init__(self, members=(), storage: str = "f16", npt: int = 0, threads: int = 0, blocks: int = 0,
                  device: str = "cuda", stochastic: bool = None, rows: int = 0, inline_bc: bool = False):
         """``npt``, ``threads`` and ``rows`` (nodes per thread, threads per tile,
-        rows per tile) default to what ``autotune`` picks for large mixed von
-        Karman batches: 1 x 64 for fx64 with 4 rows, 4 x 64 for the 16-bit
-        storages with 2 rows (rows only when the batch has enough row segments
-        to keep every SM busy with them, 1 otherwise).  Each step is a boundary-free launch
+        runs of ``threads`` chunks per tile) default to what ``autotune`` picks for large mixed von
+        Karman batches: 1 x 64 for fx64 with 4 runs, 4 x 64 for the 16-bit
+        storages with 2 runs (several runs only when the batch has enough of
+        them to keep every SM busy, 1 otherwise).  Each step is a boundary-free launch
         over every node followed by a pass over the listed boundary nodes;
         ``inline_bc`` applies the boundary sources inside the step instead
         (same results, one launch per step)."""
@@ -72,7 +73,7 @@ class Batch:
         self.npt = npt or {"fx64": 1, "f64": 2}.get(storage, 4)
         self.threads = threads or {"f16": 64, "bf16": 64, "fx64": 64}.get(storage, 128)
         self.blocks = blocks
-        self.rows = int(rows)           # rows per tile (0: chosen from the batch size)
+        self.rows = int(rows)           # runs per tile (0: chosen from the batch size)
         self.inline_bc = bool(inline_bc)
         self.bc_chunks = -1             # boundary-node plan of the work table (-1: sources in the step)
         self.gbase = torch.zeros(1, dtype=torch.int32, device=self.device)
@@ -137,15 +138,15 @@ class Batch:
 
     # -- work table ----------------------------------------------------------------
     def _rows(self) -> int:
-        """Rows per tile: the given number, else (when the batch has at least 64
-        row segments per SM) 2 for the 16-bit storages and 4 for the others,
+        """Runs per tile (a run: ``threads`` consecutive chunks of ``npt``
+        nodes, row by row): the given number, else (when the batch has at
+        least 64 runs per SM) 2 for the 16-bit storages and 4 for the others,
         else 1."""
         if self.rows > 0:
             return self.rows
-        seg = self.threads * self.npt
-        segments = sum(-(-m.nx // seg) * m.ny for m in self.members)
+        runs = sum(-(-(-(-m.nx // self.npt) * m.ny) // self.threads) for m in self.members)
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
-        if segments < 64 * sms:
+        if runs < 64 * sms:
             return 1
         return 2 if self.storage in ("f16", "bf16") else 4
 
@@ -262,7 +263,7 @@ ONE_TILE_PER_BLOCK = 1 << 24
 
 def autotune(batch: Batch, candidates=None, steps: int = 6, warmup: int = 2):
     """Pick nodes per thread, threads per block, grid size (0: one persistent
-    block per resident slot; ONE_TILE_PER_BLOCK) and rows per tile for a
+    block per resident slot; ONE_TILE_PER_BLOCK) and runs per tile for a
     batch by timing each candidate on the batch itself.  Call it before
     ``start()``: the timed steps run on the members' uninitialised buffers
     (probes off) and the global step counter is reset afterwards."""

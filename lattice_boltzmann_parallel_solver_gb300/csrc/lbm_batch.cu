@@ -57,11 +57,12 @@ int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_
     e.aux_b = L.aux_b;
     e.s0 = L.s0;
     e.s_end = L.s_end;
-    const int chunks = (L.g->nx + npt - 1) / npt;
-    e.xblocks = (chunks + threads - 1) / threads;
+    e.cpr = (L.g->nx + npt - 1) / npt;
+    e.cpr_magic = e.cpr == 1 ? 0xFFFFFFFFu : (uint32_t)((1ull << 32) / (uint64_t)e.cpr);
     e.rows = L.rows > 0 ? L.rows : 1;
     start[(size_t)j] = (int)tiles;
-    tiles += (int64_t)e.xblocks * ((L.g->ny + e.rows - 1) / e.rows);
+    const int64_t run = (int64_t)threads * e.rows;  // chunks per tile
+    tiles += ((int64_t)e.cpr * L.g->ny + run - 1) / run;
     if (e.P.g.bcmask != nullptr && (e.P.g.n_bcnodes == 0 || (L.flags & LBM_FLAG_BC_INLINE))) inline_bc = true;
     bc_start[(size_t)j] = (int)chunks_bc;
     chunks_bc += (pass_nodes(e.P.g) + kFixupChunk - 1) / kFixupChunk;

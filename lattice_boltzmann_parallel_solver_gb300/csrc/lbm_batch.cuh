@@ -98,20 +98,34 @@ __global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS,
       }
       if (g < e.s0 || g >= e.s_end) continue;
       const int local = tile - __ldg(tile_start + lo);
-      const int yb = local / e.xblocks, xb = local - yb * e.xblocks;
       const bool odd = (g - e.s0) & 1;
       const void* pin = odd ? e.pop_b : e.pop_a;
       void* pout = odd ? e.pop_a : e.pop_b;
       const void* ain = odd ? e.aux_b : e.aux_a;
       void* aout = odd ? e.aux_a : e.aux_b;
-      const int x0 = (xb * THREADS + threadIdx.x) * NPT;
       const uint32_t seed = hash32(e.P.seed + (uint32_t)(g - e.s0));
-      const int y1 = min((yb + 1) * e.rows, e.P.g.ny);
       // with the sources inside the step, lattices without the pressure rewrite
       // take the body without it; the boundary-free body leaves the rewrite to
       // the boundary-node pass
       const bool pressure = HAS_BC && e.P.g.pressure != 0;
-      for (int y = yb * e.rows; y < y1; ++y) {
+      for (int r = 0; r < e.rows; ++r) {
+        // this thread's chunk: row y, nodes x0 .. x0 + NPT - 1; the lanes of a
+        // run past the lattice's last chunk stay idle (x0 = nx).  The body
+        // takes x0 and y per thread: at a row end inside a warp the x
+        // neighbours come by direct loads, not shuffles.
+        const int c = (local * e.rows + r) * THREADS + (int)threadIdx.x;
+        const int cpr = e.cpr;
+        int y = (int)__umulhi((uint32_t)c, e.cpr_magic);
+        int xc = c - y * cpr;
+        if (xc >= cpr) {
+          xc -= cpr;
+          ++y;
+        }
+        int x0 = xc * NPT;
+        if (y >= e.P.g.ny) {
+          y = e.P.g.ny - 1;
+          x0 = e.P.g.nx;
+        }
         if constexpr (STORE == LBM_STORE_FX64) {
           if (pressure) fused_fx_body<NPT, HAS_BC, HAS_BC>(e.P, pin, pout, ain, aout, x0, y);
           else fused_fx_body<NPT, HAS_BC, false>(e.P, pin, pout, ain, aout, x0, y);
@@ -184,7 +198,6 @@ __global__ void __launch_bounds__(kFixupChunk)
 
 // one copy per translation unit (each unit launches its own)
 static __global__ void batch_advance_kernel(int* gbase, int k) { *gbase += k; }
-
 
 template <int STORE, int NPT, int THREADS, bool HAS_BC>
 inline int launch_batch(const void* table, int n, int tiles, int bc_chunks, int* gbase, int nsteps, int blocks,

@@ -533,10 +533,11 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
 
 // ---------------------------------------------------------------------------
 // Batched step: many lattices of different sizes advance one time step in one
-// launch.  The work is a flat list of tiles (one row segment of THREADS*NPT
-// nodes of one lattice); a persistent grid strides over it.  Lattice e is
-// live for global steps [s0, s_end); at global step g its input buffer is A
-// when (g - s0) is even.  g = *gbase + k, so a captured graph of launches
+// launch.  The work is a flat list of tiles; a tile is `rows` runs of THREADS
+// consecutive chunks (NPT nodes each, chunks numbered row by row, so a run may
+// cross a row end) of one lattice, and a grid strides over the list.  Lattice
+// e is live for global steps [s0, s_end); at global step g its input buffer is
+// A when (g - s0) is even.  g = *gbase + k, so a captured graph of launches
 // k = 0..K-1 followed by lbm_batch_advance stays valid across replays.
 // ---------------------------------------------------------------------------
 struct __align__(16) BatchEntry {
@@ -545,11 +546,11 @@ struct __align__(16) BatchEntry {
   void* pop_b;
   void* aux_a;
   void* aux_b;
-  int xblocks;
-  int rows;  // rows per tile
+  int cpr;             // chunks (of NPT nodes) per row
+  uint32_t cpr_magic;  // floor(2^32 / cpr), capped at 2^32 - 1: c / cpr by a multiply-high
+  int rows;            // runs of THREADS chunks per tile
   int s0, s_end;
 };
-
 
 // ---- host-side checks shared by the launchers --------------------------------
 inline bool to_geok(const lbm_geometry* g, GeoK& k) {
