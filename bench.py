@@ -473,18 +473,28 @@ def main():
 
     extras = {}
     if not args.no_extras:
-        # reduced-precision storages on the same workload
+        # the other storages on the same workload; each one's velocity error
+        # against a float64-accurate (fx64) run of the same steps
+        kv = max(50, args.steps // 2)
+        ref = make("fx64").step(5 + kv)
+        u_ref = ref.moments()[1]
+        del ref
+        torch.cuda.empty_cache()
         variants = {}
         for st in ("fx64", "f64", "f32", "f16", "bf16"):
             if st == args.storage:
                 continue
             v = make(st)
-            s, _ = timed(v, max(50, args.steps // 2), 5)
+            s, _ = timed(v, kv, 5)
             s = slowest(s)
-            variants[st] = {"mlups": world * nodes * max(50, args.steps // 2) / s / 1e6,
-                            "hbm_frac": BYTES_PER_NODE[st] * nodes / (s / max(50, args.steps // 2)) / 1e9 / hbm}
-            del v
+            u_v = v.moments()[1]
+            err = float(torch.linalg.norm(u_v - u_ref) / torch.linalg.norm(u_ref))
+            variants[st] = {"mlups": world * nodes * kv / s / 1e6,
+                            "hbm_frac": BYTES_PER_NODE[st] * nodes / (s / kv) / 1e9 / hbm,
+                            "velocity_l2_rel_err_vs_fx64": err, "steps": 5 + kv}
+            del v, u_v
             torch.cuda.empty_cache()
+        del u_ref
         extras["variants"] = variants
 
         # the other cavity sizes of the bandwidth bench

@@ -86,6 +86,7 @@ typedef struct lbm_geometry {
 #define LBM_FLAG_NPT_SHIFT 4 /* bits 4..7: nodes per thread of the vectorised kernel (0 = default) */
 #define LBM_FLAG_STOCHASTIC 256 /* 16-bit storages: round stored deviations stochastically */
 #define LBM_FLAG_BC_INLINE 1024 /* boundary sources inside the vectorised step even when g->bcnodes is set */
+#define LBM_FLAG_BC_SPLIT 2048  /* batches: the boundary-node pass even below 2^20 nodes in total */
 
 /* ---- library ------------------------------------------------------------ */
 int lbm_version(void);
@@ -222,7 +223,7 @@ typedef struct lbm_batch_lattice {
   double* probe_buf;
   int32_t* probe_count;
   uint32_t seed;  /* stochastic rounding: random bits from (seed, g - s0, node, direction) */
-  int32_t flags;  /* LBM_FLAG_STOCHASTIC, LBM_FLAG_BC_INLINE */
+  int32_t flags;  /* LBM_FLAG_STOCHASTIC, LBM_FLAG_BC_INLINE, LBM_FLAG_BC_SPLIT */
   int32_t rows;   /* runs per tile (0 = 1): a tile is `rows` runs of `threads` consecutive chunks of `npt`
                    nodes, chunks numbered row by row (a run may cross a row end) */
 } lbm_batch_lattice;
@@ -232,10 +233,12 @@ size_t lbm_batch_table_bytes(int32_t n);
  * tiles of `rows` runs of `threads` threads x `npt` nodes; synchronises `stream`.
  * *bc_chunks receives the boundary-node plan that lbm_batch_run takes: -1 when
  * the boundary sources run inside the step (some lattice has boundary nodes
- * but no list of them, or sets LBM_FLAG_BC_INLINE), else the number of
- * 128-node chunks of listed boundary nodes: each step is then a boundary-free
- * launch over every node followed by a boundary-node pass over the chunks
- * (bit-identical results, fewer registers in the hot kernel). */
+ * but no list of them or sets LBM_FLAG_BC_INLINE, or the lattices hold fewer
+ * than 2^20 nodes in total and none sets LBM_FLAG_BC_SPLIT: a second launch
+ * per step would double the fixed cost of a small batch), else the number of
+ * 128-node chunks of pass nodes: each step is then a boundary-free launch over
+ * every node followed by a boundary-node pass over the chunks (bit-identical
+ * results, fewer registers in the hot kernel). */
 int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_t threads, void* table,
                     size_t table_bytes, int32_t* total_tiles, int32_t* bc_chunks, void* stream);
 /* nsteps batched steps with `blocks` persistent blocks (0 = fill the GPU; more

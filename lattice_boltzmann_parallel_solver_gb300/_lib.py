@@ -27,6 +27,7 @@ FLAG_GENERIC = 2
 FLAG_NPT_SHIFT = 4
 FLAG_STOCHASTIC = 256
 FLAG_BC_INLINE = 1024
+FLAG_BC_SPLIT = 2048
 
 vp = C.c_void_p
 i32 = C.c_int32

@@ -56,25 +56,30 @@ class Batch:
     Members can join (``add``) and leave (``remove``) between runs."""
 
     def __init__(self, members=(), storage: str = "f16", npt: int = 0, threads: int = 0, blocks: int = 0,
-                 device: str = "cuda", stochastic: bool = None, rows: int = 0, inline_bc: bool = False):
-        """``npt``, ``threads`` and ``rows`` (nodes per thread, threads per tile,
-        runs of ``threads`` chunks per tile) default to what ``autotune`` picks for large mixed von
-        Karman batches: 1 x 64 for fx64 with 4 runs, 4 x 64 for the 16-bit
-        storages with 2 runs (several runs only when the batch has enough of
-        them to keep every SM busy, 1 otherwise).  Each step is a boundary-free launch
-        over every node followed by a pass over the listed boundary nodes;
-        ``inline_bc`` applies the boundary sources inside the step instead
-        (same results, one launch per step)."""
+                 device: str = "cuda", stochastic: bool = None, rows: int = 0, inline_bc: bool = None):
+        """Batches of at least 2^20 nodes take each step as a boundary-free
+        launch over every node followed by a pass over the boundary nodes,
+        smaller ones as one launch with the boundary sources inside (same
+        results); ``inline_bc`` True / False forces the one or the other.
+        ``npt``, ``threads`` and ``rows`` (nodes per thread, threads per tile,
+        runs of ``threads`` chunks per tile) default to what ``autotune`` picks
+        for such batches (``_default_shape``; for large mixed von Karman
+        batches 1 x 64 for fx64 with 4 runs, 4 x 64 for the 16-bit storages
+        with 2 runs; several runs only when the batch has enough of them to
+        keep every SM busy, 1 otherwise)."""
         A.require_cuda()
         self.stochastic = storage in ("f16", "bf16") if stochastic is None else bool(stochastic)
         self.storage = storage
         self.store_id, self.pop_dtype, self.aux_dtype = STORAGES[storage]
         self.device = torch.device(device)
-        self.npt = npt or {"fx64": 1, "f64": 2}.get(storage, 4)
-        self.threads = threads or {"f16": 64, "bf16": 64, "fx64": 64}.get(storage, 128)
+        # nodes per thread and threads per tile: the given ones, else chosen by
+        # the batch size each time the work table is built
+        self.inline_bc = inline_bc      # None: chosen by the batch size
+        self._auto_shape = (not npt, not threads)
+        self.npt, self.threads = int(npt), int(threads)
+        self._default_shape(0)
         self.blocks = blocks
         self.rows = int(rows)           # runs per tile (0: chosen from the batch size)
-        self.inline_bc = bool(inline_bc)
         self.bc_chunks = -1             # boundary-node plan of the work table (-1: sources in the step)
         self.gbase = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.g = 0                    # host mirror of the global step
@@ -137,6 +142,17 @@ class Batch:
         return sum(t.numel() * t.element_size() for m in self.members for t in m.pop + m.aux)
 
     # -- work table ----------------------------------------------------------------
+    def _default_shape(self, nodes: int):
+        """Default nodes per thread / threads per tile: below 2^20 nodes (one
+        launch per step, boundary sources inside) 2 x 64 for the 16-bit
+        storages and 1 x 128 for fx64; above (boundary-free step and the
+        boundary-node pass) 4 x 64 and 1 x 64."""
+        split = self.inline_bc is False or (self.inline_bc is None and nodes >= (1 << 20))
+        if self._auto_shape[0]:
+            self.npt = {"fx64": 1, "f64": 2, "f16": 4 if split else 2, "bf16": 4 if split else 2}.get(self.storage, 4)
+        if self._auto_shape[1]:
+            self.threads = {"f16": 64, "bf16": 64, "fx64": 64 if split else 128}.get(self.storage, 128)
+
     def _rows(self) -> int:
         """Runs per tile (a run: ``threads`` consecutive chunks of ``npt``
         nodes, row by row): the given number, else (when the batch has at
@@ -152,6 +168,7 @@ class Batch:
 
     def _build(self, with_probes=True):
         n = len(self.members)
+        self._default_shape(self.nodes)
         rows = self._rows()
         arr = (BatchLatticeC * n)()
         self._keep = []
@@ -170,7 +187,7 @@ class Batch:
                 c.probe_x = c.probe_y = -1
             c.seed = int(m.seed) & 0xFFFFFFFF
             c.flags = (_lib.FLAG_STOCHASTIC if self.stochastic else 0) | \
-                (_lib.FLAG_BC_INLINE if self.inline_bc else 0)
+                {True: _lib.FLAG_BC_INLINE, False: _lib.FLAG_BC_SPLIT}.get(self.inline_bc, 0)
             c.rows = rows
         size = int(_lib.load().lbm_batch_table_bytes(n))
         self.table = torch.empty(size, dtype=torch.uint8, device=self.device)
@@ -277,6 +294,7 @@ def autotune(batch: Batch, candidates=None, steps: int = 6, warmup: int = 2):
         npt, threads, blocks = cand[:3]
         rows = cand[3] if len(cand) > 3 else 1
         batch.npt, batch.threads, batch.blocks, batch.rows = npt, threads, blocks, rows
+        batch._auto_shape = (False, False)
         try:
             batch._build(with_probes=False)
         except (AssertionError, NotImplementedError):

@@ -23,8 +23,9 @@ int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_
   if ((uintptr_t)table % 16 != 0) return set_error(LBM_ERR_ARG, "batch table must be 16-byte aligned");
   std::vector<BatchEntry> ent((size_t)n);
   std::vector<int> start((size_t)n), bc_start((size_t)n);
-  int64_t tiles = 0, chunks_bc = 0;
+  int64_t tiles = 0, chunks_bc = 0, nodes = 0;
   bool inline_bc = false;  // some lattice has boundary nodes but no list of them
+  bool force_split = false;
   for (int j = 0; j < n; ++j) {
     const lbm_batch_lattice& L = lat[j];
     BatchEntry& e = ent[(size_t)j];
@@ -64,6 +65,8 @@ int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_
     const int64_t run = (int64_t)threads * e.rows;  // chunks per tile
     tiles += ((int64_t)e.cpr * L.g->ny + run - 1) / run;
     if (e.P.g.bcmask != nullptr && (e.P.g.n_bcnodes == 0 || (L.flags & LBM_FLAG_BC_INLINE))) inline_bc = true;
+    if (L.flags & LBM_FLAG_BC_SPLIT) force_split = true;
+    nodes += (int64_t)L.g->nx * L.g->ny;
     bc_start[(size_t)j] = (int)chunks_bc;
     chunks_bc += (pass_nodes(e.P.g) + kFixupChunk - 1) / kFixupChunk;
   }
@@ -79,6 +82,8 @@ int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_
   if (err == cudaSuccess) err = cudaStreamSynchronize((cudaStream_t)stream);
   if (err != cudaSuccess) return set_error(LBM_ERR_CUDA, cudaGetErrorString(err));
   *total_tiles = (int32_t)tiles;
+  // small batches keep one launch per step (the pass would double their fixed cost)
+  if (nodes < kBatchSplitNodes && !force_split) inline_bc = true;
   *bc_chunks = inline_bc ? -1 : (int32_t)chunks_bc;
   return LBM_OK;
 }

@@ -149,6 +149,10 @@ __global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS,
 // chunks [bc_start[j], bc_start[j + 1]) of kFixupChunk pass nodes.
 constexpr int kFixupChunk = 128;
 
+// batches below this many nodes in total keep the sources inside one launch
+// per step, as single lattices do
+constexpr int64_t kBatchSplitNodes = (int64_t)1 << 20;
+
 inline int64_t pass_nodes(const GeoK& g) {
   return (g.bcmask != nullptr ? (int64_t)g.n_bcnodes : 0) + (g.pressure ? 2 * (int64_t)g.ny : 0);
 }
