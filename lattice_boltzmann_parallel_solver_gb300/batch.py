@@ -144,14 +144,16 @@ class Batch:
     # -- work table ----------------------------------------------------------------
     def _default_shape(self, nodes: int):
         """Default nodes per thread / threads per tile: below 2^20 nodes (one
-        launch per step, boundary sources inside) 2 x 64 for the 16-bit
-        storages and 1 x 128 for fx64; above (boundary-free step and the
-        boundary-node pass) 4 x 64 and 1 x 64."""
+        launch per step, boundary sources inside, row-segment tiles) 2 x 128
+        for the 16-bit storages and 1 x 128 for fx64; above (boundary-free step
+        over runs across row ends, then the boundary-node pass) 4 x 64 and
+        1 x 64."""
         split = self.inline_bc is False or (self.inline_bc is None and nodes >= (1 << 20))
         if self._auto_shape[0]:
             self.npt = {"fx64": 1, "f64": 2, "f16": 4 if split else 2, "bf16": 4 if split else 2}.get(self.storage, 4)
         if self._auto_shape[1]:
-            self.threads = {"f16": 64, "bf16": 64, "fx64": 64 if split else 128}.get(self.storage, 128)
+            self.threads = {"f16": 64 if split else 128, "bf16": 64 if split else 128,
+                            "fx64": 64 if split else 128}.get(self.storage, 128)
 
     def _rows(self) -> int:
         """Runs per tile (a run: ``threads`` consecutive chunks of ``npt``

@@ -60,15 +60,26 @@ int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_
     e.s_end = L.s_end;
     e.cpr = (L.g->nx + npt - 1) / npt;
     e.cpr_magic = e.cpr == 1 ? 0xFFFFFFFFu : (uint32_t)((1ull << 32) / (uint64_t)e.cpr);
+    e.xblocks = (e.cpr + threads - 1) / threads;
     e.rows = L.rows > 0 ? L.rows : 1;
-    start[(size_t)j] = (int)tiles;
-    const int64_t run = (int64_t)threads * e.rows;  // chunks per tile
-    tiles += ((int64_t)e.cpr * L.g->ny + run - 1) / run;
     if (e.P.g.bcmask != nullptr && (e.P.g.n_bcnodes == 0 || (L.flags & LBM_FLAG_BC_INLINE))) inline_bc = true;
     if (L.flags & LBM_FLAG_BC_SPLIT) force_split = true;
     nodes += (int64_t)L.g->nx * L.g->ny;
     bc_start[(size_t)j] = (int)chunks_bc;
     chunks_bc += (pass_nodes(e.P.g) + kFixupChunk - 1) / kFixupChunk;
+  }
+  // small batches keep one launch per step (the pass would double their fixed cost)
+  if (nodes < kBatchSplitNodes && !force_split) inline_bc = true;
+  // tiles: runs across row ends with the pass, row segments without it
+  for (int j = 0; j < n; ++j) {
+    const BatchEntry& e = ent[(size_t)j];
+    start[(size_t)j] = (int)tiles;
+    if (inline_bc) {
+      tiles += (int64_t)e.xblocks * ((e.P.g.ny + e.rows - 1) / e.rows);
+    } else {
+      const int64_t run = (int64_t)threads * e.rows;
+      tiles += ((int64_t)e.cpr * e.P.g.ny + run - 1) / run;
+    }
   }
   if (tiles >= ((int64_t)1 << 31) || chunks_bc >= ((int64_t)1 << 31))
     return set_error(LBM_ERR_ARG, "too many tiles");
@@ -82,8 +93,6 @@ int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_
   if (err == cudaSuccess) err = cudaStreamSynchronize((cudaStream_t)stream);
   if (err != cudaSuccess) return set_error(LBM_ERR_CUDA, cudaGetErrorString(err));
   *total_tiles = (int32_t)tiles;
-  // small batches keep one launch per step (the pass would double their fixed cost)
-  if (nodes < kBatchSplitNodes && !force_split) inline_bc = true;
   *bc_chunks = inline_bc ? -1 : (int32_t)chunks_bc;
   return LBM_OK;
 }

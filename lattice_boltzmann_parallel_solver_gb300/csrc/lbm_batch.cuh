@@ -108,30 +108,44 @@ __global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS,
       // take the body without it; the boundary-free body leaves the rewrite to
       // the boundary-node pass
       const bool pressure = HAS_BC && e.P.g.pressure != 0;
-      for (int r = 0; r < e.rows; ++r) {
-        // this thread's chunk: row y, nodes x0 .. x0 + NPT - 1; the lanes of a
-        // run past the lattice's last chunk stay idle (x0 = nx).  The body
-        // takes x0 and y per thread: at a row end inside a warp the x
-        // neighbours come by direct loads, not shuffles.
-        const int c = (local * e.rows + r) * THREADS + (int)threadIdx.x;
-        const int cpr = e.cpr;
-        int y = (int)__umulhi((uint32_t)c, e.cpr_magic);
-        int xc = c - y * cpr;
-        if (xc >= cpr) {
-          xc -= cpr;
-          ++y;
-        }
-        int x0 = xc * NPT;
-        if (y >= e.P.g.ny) {
-          y = e.P.g.ny - 1;
-          x0 = e.P.g.nx;
-        }
+      auto step_chunk = [&](int x0, int y) {
         if constexpr (STORE == LBM_STORE_FX64) {
           if (pressure) fused_fx_body<NPT, HAS_BC, HAS_BC>(e.P, pin, pout, ain, aout, x0, y);
           else fused_fx_body<NPT, HAS_BC, false>(e.P, pin, pout, ain, aout, x0, y);
         } else {
           if (pressure) fused_v2_body<STORE, NPT, HAS_BC, HAS_BC>(e.P, pin, pout, ain, aout, x0, y, seed);
           else fused_v2_body<STORE, NPT, HAS_BC, false>(e.P, pin, pout, ain, aout, x0, y, seed);
+        }
+      };
+      if constexpr (HAS_BC) {
+        // row-segment tiles (small batches): `rows` rows of one segment of
+        // THREADS chunks; the row is uniform over the block, so its addressing
+        // runs in the uniform datapath (on a lone 420x180 lattice 15 % faster
+        // than runs across row ends)
+        const int yb = local / e.xblocks, xb = local - yb * e.xblocks;
+        const int x0 = (xb * THREADS + (int)threadIdx.x) * NPT;
+        const int y1 = min((yb + 1) * e.rows, e.P.g.ny);
+        for (int y = yb * e.rows; y < y1; ++y) step_chunk(x0, y);
+      } else {
+        // runs of THREADS consecutive chunks, chunks numbered row by row: no
+        // idle lanes at row ends.  The lanes of a run past the lattice's last
+        // chunk stay idle (x0 = nx).  The body takes x0 and y per thread: at a
+        // row end inside a warp the x neighbours come by direct loads.
+        for (int r = 0; r < e.rows; ++r) {
+          const int c = (local * e.rows + r) * THREADS + (int)threadIdx.x;
+          const int cpr = e.cpr;
+          int y = (int)__umulhi((uint32_t)c, e.cpr_magic);
+          int xc = c - y * cpr;
+          if (xc >= cpr) {
+            xc -= cpr;
+            ++y;
+          }
+          int x0 = xc * NPT;
+          if (y >= e.P.g.ny) {
+            y = e.P.g.ny - 1;
+            x0 = e.P.g.nx;
+          }
+          step_chunk(x0, y);
         }
       }
     }

@@ -533,12 +533,14 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
 
 // ---------------------------------------------------------------------------
 // Batched step: many lattices of different sizes advance one time step in one
-// launch.  The work is a flat list of tiles; a tile is `rows` runs of THREADS
-// consecutive chunks (NPT nodes each, chunks numbered row by row, so a run may
-// cross a row end) of one lattice, and a grid strides over the list.  Lattice
-// e is live for global steps [s0, s_end); at global step g its input buffer is
-// A when (g - s0) is even.  g = *gbase + k, so a captured graph of launches
-// k = 0..K-1 followed by lbm_batch_advance stays valid across replays.
+// launch.  The work is a flat list of tiles of one lattice each, and a grid
+// strides over the list.  With the boundary-node pass (large batches) a tile
+// is `rows` runs of THREADS consecutive chunks (NPT nodes each, chunks
+// numbered row by row, so a run may cross a row end); with the sources inside
+// the step (small batches) it is `rows` rows of one segment of THREADS chunks.
+// Lattice e is live for global steps [s0, s_end); at global step g its input
+// buffer is A when (g - s0) is even.  g = *gbase + k, so a captured graph of
+// launches k = 0..K-1 followed by lbm_batch_advance stays valid across replays.
 // ---------------------------------------------------------------------------
 struct __align__(16) BatchEntry {
   KParams P;
@@ -548,7 +550,8 @@ struct __align__(16) BatchEntry {
   void* aux_b;
   int cpr;             // chunks (of NPT nodes) per row
   uint32_t cpr_magic;  // floor(2^32 / cpr), capped at 2^32 - 1: c / cpr by a multiply-high
-  int rows;            // runs of THREADS chunks per tile
+  int xblocks;         // row segments of THREADS chunks per row
+  int rows;            // runs (or rows) per tile
   int s0, s_end;
 };
 
