@@ -598,6 +598,9 @@ inline int check_pitch(int nx, int64_t pitch) {
 inline bool v2_fits(const KParams& P, int npt) {
   const int nx = P.g.nx;
   if (nx < npt + 2 || P.g.ny > 65535) return false;
+  // the vectorised bodies give each node at most one pressure rewrite; on a
+  // 3-column lattice column 1 is both nx-2 and 1 and owes two
+  if (P.g.pressure && nx < 4) return false;
   if (9 * P.plane >= ((int64_t)1 << 31) || P.pitch % npt != 0 || P.pitch < (nx + npt - 1) / npt * npt) return false;
   if (((uintptr_t)P.pop_in | (uintptr_t)P.pop_out) % 16 != 0) return false;
   return true;

@@ -132,3 +132,62 @@ def test_boundary_node_pass_equals_inline_sources(pkg, storage):
         if m.probe is not None:
             ta, tb = a.probe_trace(j), b.probe_trace(j)
             assert ta.shape[0] == m.steps - 1 and torch.equal(ta, tb), (storage, j)
+
+
+def test_batch_plan_follows_the_size(pkg):
+    """Below 2^20 nodes in total a batch keeps the boundary sources inside one
+    launch per step; from 2^20 it runs the boundary-free step and the pass."""
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch, Member
+    S = pkg.scenarios
+    f, rho, u, bnd = S.cavity(64)
+    small = Batch([Member(64, 64, 1.7, bnd, steps=3, f0=f, rho0=rho, u0=u)], storage="f16").start()
+    assert small.bc_chunks == -1
+    big_nodes = 1056 * 1000
+    rho, u = np.ones((1056, 1000)), np.zeros((1056, 1000, 2))
+    bnd = pkg.boundary_utils.cavity_boundary_conditions(1056, 1000, 0.1, 1.0)
+    big = Batch([Member(1056, 1000, 1.7, bnd, steps=3, f0=S.equilibrium_np(rho, u), rho0=rho, u0=u)],
+                storage="fx64").start()
+    assert big.nodes == big_nodes >= 1 << 20 and big.bc_chunks > 0
+    big.run()
+    ref = alone(pkg, big.members[0], "fx64", big.npt).read()[0]
+    assert float((big.read(0)[0] - ref).abs().max() / ref.abs().max()) <= 1e-13
+
+
+@pytest.mark.parametrize("nx", [4, 5])
+def test_pass_pressure_columns_on_narrow_lattices(pkg, nx):
+    """Under the pressure rewrite the pass recomputes columns 1 and nx-2; on
+    4- and 5-column lattices (adjacent columns, one between) the split step
+    still equals the step with the sources inside it."""
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch, Member
+    U, S = pkg.boundary_utils, pkg.scenarios
+    runs = []
+    for inline in (True, False):
+        rho, u = np.ones((nx, 12)), np.zeros((nx, 12, 2))
+        bnd = U.poiseuille_flow_boundary_conditions(nx, 12, (1 + 3e-3) / 3, (1 - 3e-3) / 3)
+        m = Member(nx, 12, 1.3, bnd, steps=25, f0=S.equilibrium_np(rho, u), rho0=rho, u0=u, probe=(1, 5))
+        b = Batch([m], storage="fx64", npt=1, threads=64, inline_bc=inline).start()
+        b.run()
+        runs.append(b)
+    a, b = runs
+    assert torch.equal(a.read(0)[0], b.read(0)[0])
+    assert torch.equal(a.probe_trace(0), b.probe_trace(0)) and a.probe_trace(0).shape[0] == 24
+
+
+def test_three_column_pressure_lattice(pkg):
+    """On a 3-column lattice under the pressure rewrite column 1 feeds both
+    column 0 (inlet side) and column 2 (outlet side), as in the reference: a
+    resident lattice takes the one-node-per-thread kernel and matches the
+    oracle, and a batch, whose vectorised bodies give a node one rewrite,
+    refuses the lattice."""
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch, Member
+    U, S = pkg.boundary_utils, pkg.scenarios
+    p_in, p_out = (1 + 3e-3) / 3, (1 - 3e-3) / 3
+    rho, u = np.ones((3, 12)), np.zeros((3, 12, 2))
+    f0 = S.equilibrium_np(rho, u)
+    ref = O.run(f0, rho, u, 1.3, 25, O.poiseuille_boundary(3, 12, p_in, p_out))
+    bnd = U.poiseuille_flow_boundary_conditions(3, 12, p_in, p_out)
+    for storage in ("fx64", "f64"):
+        got = pkg.Lattice(3, 12, 1.3, bnd, storage=storage).set_state(f0, rho, u).step(25).read()[0].cpu().numpy()
+        assert np.abs(got - ref[0]).max() / np.abs(ref[0]).max() <= 1e-12, storage
+    with pytest.raises(NotImplementedError):
+        Batch([Member(3, 12, 1.3, bnd, steps=5, f0=f0, rho0=rho, u0=u)], storage="fx64", npt=1).start()
