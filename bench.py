@@ -333,7 +333,7 @@ def _cpu_worker(args):
     return n * n * steps, time.perf_counter() - t0
 
 
-def cpu_baseline_single(n=1024, steps=3):
+def cpu_baseline_single(n=1024, steps=40):
     nodes, dt = _cpu_worker((n, steps, 1))
     return {"value": nodes / dt / 1e6, "unit": "MLUPS", "cores": 1, "kind": "port",
             "sample": "NumPy oracle, one process, cavity %dx%d, %d steps after 1 warm-up step" % (n, n, steps)}

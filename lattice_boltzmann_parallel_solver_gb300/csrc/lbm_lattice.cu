@@ -284,11 +284,12 @@ static int launch_fx(const KParams& P, cudaStream_t s) {
   return check_launch("fused_fx_kernel");
 }
 
+// nodes per thread, measured on the 8192^2 cavity: float32 87.7 GLUPS at 4
+// against 83.6 at 2; 16-bit 168 at 4 against 160 at 8 (512 threads per SM)
 static int default_npt(int storage) {
   switch (storage) {
     case LBM_STORE_F64: return 2;
     case LBM_STORE_FX64: return 1;
-    case LBM_STORE_F32: return 2;
     default: return 4;
   }
 }
