@@ -67,9 +67,11 @@ typedef struct lbm_geometry {
   double rho_in, rho_out;
   int32_t outlet; /* some node uses LBM_SRC_OUTLET */
   /* device, the n_bcnodes linear indices y*nx + x (ascending) of the nodes with a
-   * bcmask bit.  With it the vectorised step runs its boundary-free body over the
-   * whole lattice and then recomputes just these nodes with their sources; NULL
-   * (or LBM_FLAG_BC_INLINE) applies the sources inside the step. */
+   * bcmask bit.  With it, on lattices of at least 2^22 nodes in the 16-bit
+   * storages and 2^25 in the others (or with LBM_FLAG_BC_SPLIT), the vectorised
+   * step runs its boundary-free body over the whole lattice and then recomputes
+   * just these nodes with their sources; NULL, a smaller lattice or
+   * LBM_FLAG_BC_INLINE applies the sources inside the step. */
   const int32_t* bcnodes;
   int32_t n_bcnodes;
 } lbm_geometry;
@@ -86,7 +88,7 @@ typedef struct lbm_geometry {
 #define LBM_FLAG_NPT_SHIFT 4 /* bits 4..7: nodes per thread of the vectorised kernel (0 = default) */
 #define LBM_FLAG_STOCHASTIC 256 /* 16-bit storages: round stored deviations stochastically */
 #define LBM_FLAG_BC_INLINE 1024 /* boundary sources inside the vectorised step even when g->bcnodes is set */
-#define LBM_FLAG_BC_SPLIT 2048  /* batches: the boundary-node pass even below 2^20 nodes in total */
+#define LBM_FLAG_BC_SPLIT 2048  /* the boundary-node pass even below the size from which it is taken by default */
 
 /* ---- library ------------------------------------------------------------ */
 int lbm_version(void);

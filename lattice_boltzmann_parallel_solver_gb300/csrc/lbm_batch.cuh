@@ -164,7 +164,7 @@ __global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS,
 constexpr int kFixupChunk = 128;
 
 // batches below this many nodes in total keep the sources inside one launch
-// per step, as single lattices do
+// per step (a second launch per step would double a small batch's fixed cost)
 constexpr int64_t kBatchSplitNodes = (int64_t)1 << 20;
 
 inline int64_t pass_nodes(const GeoK& g) {

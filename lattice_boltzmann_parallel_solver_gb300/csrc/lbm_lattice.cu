@@ -318,19 +318,25 @@ static int launch_fixup(const KParams& P, cudaStream_t s) {
 
 static int launch_fused_step(int storage, int npt, int flags, const KParams& P, cudaStream_t s);
 
-// One step.  On lattices of at least kSplitNodes nodes whose geometry lists its
-// boundary nodes (at most an eighth of the lattice), the vectorised kernel runs
-// without boundary work: the body's boundary block then stays out of the hot
-// loop (it costs registers under the 64-register cap), and the listed nodes are
-// recomputed by the boundary-node pass.  Smaller lattices keep one launch per
-// step, whose fixed cost would otherwise double.
-constexpr int64_t kSplitNodes = (int64_t)1 << 20;
+// One step.  On large lattices whose geometry lists its boundary nodes (at most
+// an eighth of the lattice), the vectorised kernel runs without boundary work:
+// the body's boundary block then stays out of the hot loop (it costs registers
+// under the 64-register cap), and the listed nodes are recomputed by the
+// boundary-node pass.  Smaller lattices keep one launch per step, whose fixed
+// cost would otherwise outweigh the gain.  Measured on the cavity (split against
+// inline GLUPS): the 16-bit storages gain from 2896^2 on (132 against 124) and
+// lose below 2048^2 (64 against 85 at 1024^2); the other storages gain only at
+// 8192^2 (fx64 46.9 against 46.5) and lose or tie up to 4096^2.
+static int64_t split_nodes(int storage) {
+  return (storage == LBM_STORE_F16S || storage == LBM_STORE_BF16S) ? (int64_t)1 << 22 : (int64_t)1 << 25;
+}
 
 static int launch_fused(int storage, int flags, const KParams& P, cudaStream_t s) {
   const int npt = v2_npt(storage, flags, P);
   const int64_t nodes = (int64_t)P.g.nx * P.g.ny;
   const bool split = npt > 0 && !(flags & LBM_FLAG_BC_INLINE) && P.g.bcmask != nullptr && P.g.n_bcnodes > 0 &&
-                     nodes >= kSplitNodes && (int64_t)P.g.n_bcnodes * 8 <= nodes;
+                     (nodes >= split_nodes(storage) || (flags & LBM_FLAG_BC_SPLIT)) &&
+                     (int64_t)P.g.n_bcnodes * 8 <= nodes;
   if (!split) return launch_fused_step(storage, npt, flags, P, s);
   KParams Q = P;
   Q.g.bcmask = nullptr;

@@ -41,14 +41,17 @@ class Lattice:
 
     def __init__(self, nx: int, ny: int, omega: float, boundary=None, storage: str = None,
                  exact: bool = False, device: str = "cuda", generic: bool = False, npt: int = 0,
-                 stochastic: bool = None, seed: int = 0, bc_inline: bool = False):
+                 stochastic: bool = None, seed: int = 0, bc_inline: bool = None):
         """``generic`` forces the one-node-per-thread kernel; ``npt`` sets the
         nodes per thread of the vectorised kernel (0 = the default for the storage).
         ``stochastic`` (default: on for the 16-bit storages) rounds the stored
         deviations stochastically, which keeps increments smaller than half a
         16-bit step from being lost; ``seed`` seeds its random bits.
-        ``bc_inline`` applies the boundary sources inside the vectorised step
-        instead of in a separate pass over the boundary nodes (same results).  The
+        Large lattices (from 2^22 nodes in the 16-bit storages, 2^25 in the
+        others) run the vectorised step without boundary work and then a pass
+        over the boundary nodes; smaller ones apply the boundary sources inside
+        the step (same results).  ``bc_inline`` True / False forces the one or
+        the other.  The
         default storage is "fx64", or "f64" with ``exact`` (the reference's
         float64 operation order, bit for bit)."""
         A.require_cuda()
@@ -64,7 +67,7 @@ class Lattice:
             stochastic = storage in ("f16", "bf16")
         self.flags = (_lib.FLAG_EXACT if exact else 0) | (_lib.FLAG_GENERIC if generic else 0) | \
             ((int(npt) & 15) << _lib.FLAG_NPT_SHIFT) | (_lib.FLAG_STOCHASTIC if stochastic else 0) | \
-            (_lib.FLAG_BC_INLINE if bc_inline else 0)
+            {True: _lib.FLAG_BC_INLINE, False: _lib.FLAG_BC_SPLIT}.get(bc_inline, 0)
         self.seed = int(seed) & 0xFFFFFFFF
         self.pitch = (self.nx + 31) // 32 * 32
         self.device = torch.device(device)

@@ -147,12 +147,12 @@ def test_boundary_node_pass_equals_inline_sources(pkg, storage, name):
     """The step as a boundary-free pass over every node plus a pass over the
     listed boundary nodes gives the same bits as the boundary sources applied
     inside the step (moments of the last step included)."""
-    nx, ny = 1024, 1024  # the boundary-node pass applies from 2^20 nodes
+    nx, ny = 1024, 1024  # below the default size of the pass: forced
     bnd = dict(geometries(pkg, nx, ny))[name]
     geo = bnd.geometry(nx, ny)
     assert 0 < geo.struct.n_bcnodes * 8 <= nx * ny
     f, rho, u = start(nx, ny, 21)
-    a = pkg.Lattice(nx, ny, 1.3, bnd, storage=storage).set_state(f, rho, u).step(30)
+    a = pkg.Lattice(nx, ny, 1.3, bnd, storage=storage, bc_inline=False).set_state(f, rho, u).step(30)
     b = pkg.Lattice(nx, ny, 1.3, bnd, storage=storage, bc_inline=True).set_state(f, rho, u).step(30)
     for x, y in zip(a.read(), b.read()):
         assert torch.equal(x, y)
