@@ -1,7 +1,8 @@
 // lbm_batch.cuh -- the batched step kernels and their launcher (many lattices
-// of different sizes advanced by one launch per time step).  Two translation
-// units instantiate the launcher: lbm_batch_inline.cu (boundary sources inside
-// the step) and lbm_batch_split.cu (boundary-free step + boundary-node pass).
+// of different sizes advanced together, one or two launches per time step).
+// Two translation units instantiate the launcher: lbm_batch_inline.cu
+// (boundary sources inside the step) and lbm_batch_split.cu (boundary-free
+// step + boundary-node pass).
 #pragma once
 #include <algorithm>
 #include <cstddef>
