@@ -40,6 +40,9 @@ def parse():
     p.add_argument("--n", type=int, default=8192, help="cavity side")
     p.add_argument("--storage", default="fx64", choices=sorted(BYTES_PER_NODE))
     p.add_argument("--exact", action="store_true", help="NumPy-order float64 arithmetic")
+    p.add_argument("--bc", default="auto", choices=["auto", "split", "inline"],
+                   help="boundary sources: a separate pass over the boundary nodes (split), inside the step "
+                        "(inline), or chosen by the lattice size (auto)")
     p.add_argument("--no-extras", action="store_true", help="skip variants, e2e, CPU baseline and the other configs")
     p.add_argument("--workload", default="cavity", choices=["cavity", "shear", "vk", "batch", "serve", "batch_step"],
                    help="cavity: the headline line; the others print one config's results and exit")
@@ -437,8 +440,10 @@ def main():
     bnd = cavity_boundary_conditions(n, n, 0.1, 1.0)
     w = torch.tensor([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4, dtype=torch.float64, device="cuda")
 
+    bc_inline = {"auto": None, "split": False, "inline": True}[args.bc]
+
     def make(storage, exact=False):
-        lat = P.Lattice(n, n, 1.7, bnd, storage=storage, exact=exact)
+        lat = P.Lattice(n, n, 1.7, bnd, storage=storage, exact=exact, bc_inline=bc_inline)
         f0 = w.expand(n, n, 9).contiguous()  # equilibrium at rho = 1, u = 0
         lat.set_state(f0)
         del f0
