@@ -56,7 +56,7 @@ class Batch:
     Members can join (``add``) and leave (``remove``) between runs."""
 
     def __init__(self, members=(), storage: str = "f16", npt: int = 0, threads: int = 0, blocks: int = 0,
-                 device: str = "cuda", stochastic: bool = None, rows: int = 0, inline_bc: bool = None):
+                 device: str = "cuda", stochastic: bool = None, rows: int = 0, inline_bc: bool | None = None):
         """Batches of at least 2^20 nodes take each step as a boundary-free
         launch over every node followed by a pass over the boundary nodes,
         smaller ones as one launch with the boundary sources inside (same

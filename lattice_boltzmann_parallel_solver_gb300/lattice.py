@@ -41,7 +41,7 @@ class Lattice:
 
     def __init__(self, nx: int, ny: int, omega: float, boundary=None, storage: str = None,
                  exact: bool = False, device: str = "cuda", generic: bool = False, npt: int = 0,
-                 stochastic: bool = None, seed: int = 0, bc_inline: bool = None):
+                 stochastic: bool = None, seed: int = 0, bc_inline: bool | None = None):
         """``generic`` forces the one-node-per-thread kernel; ``npt`` sets the
         nodes per thread of the vectorised kernel (0 = the default for the storage).
         ``stochastic`` (default: on for the 16-bit storages) rounds the stored
