@@ -69,3 +69,56 @@ def test_geometry_struct_layout_matches_c(tmp_path):
     assert int(out["size"]) == ctypes.sizeof(_lib.Geometry)
     for n in fields:
         assert int(out[n]) == getattr(_lib.Geometry, n).offset, n
+
+
+@pytest.mark.skipif(shutil.which("gcc") is None, reason="gcc not available")
+def test_batch_lattice_struct_layout_matches_c(tmp_path):
+    src = tmp_path / "batch_layout.c"
+    fields = [f[0] for f in _lib.BatchLattice._fields_]
+    body = "".join('printf("%s %%zu\\n", offsetof(lbm_batch_lattice, %s));' % (n, n) for n in fields)
+    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "lbm_gb300.h"\n'
+                   'int main(void){printf("size %%zu\\n", sizeof(lbm_batch_lattice));%s return 0;}\n' % body)
+    exe = tmp_path / "batch_layout"
+    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    out = dict(line.split() for line in subprocess.check_output([str(exe)]).decode().splitlines())
+    assert int(out["size"]) == ctypes.sizeof(_lib.BatchLattice)
+    for n in fields:
+        assert int(out[n]) == getattr(_lib.BatchLattice, n).offset, n
+
+
+def test_batch_argument_errors_without_gpu(lib):
+    # the batch table builder checks its arguments before any CUDA call
+    assert lib.lbm_batch_table_bytes(8) > lib.lbm_batch_table_bytes(4) > lib.lbm_batch_table_bytes(1) > 0
+    g = _lib.Geometry()
+    g.nx, g.ny = 64, 16
+    arr = (_lib.BatchLattice * 1)()
+    arr[0].g = ctypes.addressof(g)
+    arr[0].pop_a, arr[0].pop_b, arr[0].pitch, arr[0].omega = 1024, 2048, 64, 1.0
+    size = int(lib.lbm_batch_table_bytes(1))
+    table = ctypes.create_string_buffer(size + 16)
+    ptr = (ctypes.addressof(table) + 15) // 16 * 16
+    tiles, chunks = ctypes.c_int32(0), ctypes.c_int32(0)
+
+    def build(n=1, npt=4, threads=64, nbytes=size, with_chunks=True):
+        return lib.lbm_batch_build(arr, n, npt, threads, ptr, nbytes, ctypes.byref(tiles),
+                                   ctypes.byref(chunks) if with_chunks else None, None)
+
+    with pytest.raises(AssertionError, match="bad batch arguments"):
+        _lib.check(build(n=0))
+    with pytest.raises(AssertionError, match="bad batch arguments"):
+        _lib.check(build(with_chunks=False))
+    with pytest.raises(AssertionError, match="too small"):
+        _lib.check(build(nbytes=size - 1))
+    with pytest.raises(AssertionError, match="npt"):
+        _lib.check(build(npt=3))
+    arr[0].omega = 2.0
+    with pytest.raises(AssertionError, match="omega"):
+        _lib.check(build())
+    arr[0].omega, arr[0].pitch = 1.0, 60
+    with pytest.raises(AssertionError, match="pitch"):
+        _lib.check(build())
+    arr[0].pitch, g.nx = 64, 5  # narrower than npt + 2 nodes
+    with pytest.raises(NotImplementedError):
+        _lib.check(build())
+    with pytest.raises(AssertionError, match="batch run"):
+        _lib.check(lib.lbm_batch_run(ptr, 1, 10, -1, 2, 4, 64, None, 1, 0, None))
