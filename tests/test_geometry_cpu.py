@@ -144,3 +144,27 @@ def test_too_many_constant_sets():
         src.append((m, 2, CONST, 0.01 * x))
     with pytest.raises(NotImplementedError):
         CompiledGeometry(lx, ly, src, device="cpu")
+
+
+@pytest.mark.parametrize("name", ["couette", "poiseuille", "cavity", "vk"])
+def test_boundary_node_list_matches_the_mask(name):
+    """The boundary-node pass recomputes exactly the listed nodes: the list
+    holds the linear indices y*nx + x of the mask's set bits, ascending, and
+    covers at most an eighth of these lattices."""
+    lx, ly = 70, 33
+    if name == "couette":
+        b = BU.couette_flow_boundary_conditions(lx, ly, 0.05, 1.0)
+    elif name == "poiseuille":
+        b = BU.poiseuille_flow_boundary_conditions(lx, ly, 0.34, 0.33)
+    elif name == "cavity":
+        b = BU.cavity_boundary_conditions(lx, ly, 0.1, 1.0)
+    else:
+        feq_in = O.inlet_populations((1, 1), 1.0, 0.1)[0, 0]
+        b = BU.Boundary(BU._vk_closures(lx, ly, 1.0, 0.1, 8, feq_in=feq_in))
+    g = compiled(b, lx, ly)
+    mask = g.bcmask.cpu().numpy()
+    bits = ((mask[:, :, None] >> np.arange(32, dtype=np.uint32)) & 1).reshape(ly, -1)[:, :lx].astype(bool)
+    want = np.flatnonzero(bits.reshape(-1))
+    got = g.bcnodes.cpu().numpy()
+    assert got.dtype == np.int32 and np.array_equal(got, want)
+    assert g.struct.n_bcnodes == want.size and 0 < want.size * 8 <= lx * ly
