@@ -81,7 +81,7 @@ typedef struct lbm_geometry {
 #define LBM_STORE_F32 1   /* 36 B per node */
 #define LBM_STORE_F16S 2  /* 18 B per node, f_i - w_i in binary16 */
 #define LBM_STORE_BF16S 3 /* 18 B per node, f_i - w_i in bfloat16 */
-#define LBM_STORE_FX64 4  /* 72 B per node, round(f_i 2^53) in int64: float64 accuracy, no float64 arithmetic */
+#define LBM_STORE_FX64 4  /* 72 B per node, round((f_i - w_i) 2^56) in int64: float64 accuracy, no float64 arithmetic */
 
 #define LBM_FLAG_EXACT 1  /* float64 arithmetic in the reference's NumPy operation order, no FMA contraction */
 #define LBM_FLAG_GENERIC 2 /* use the one-node-per-thread kernel instead of the vectorised one */
@@ -183,6 +183,32 @@ int lbm_lattice_init(const lbm_geometry* g, int32_t storage, const double* f, co
 int lbm_lattice_run(const lbm_geometry* g, int32_t storage, void* pop_a, void* pop_b, int64_t pitch,
                     void* aux_a, void* aux_b, double omega, int32_t nsteps, double* rho_out,
                     double* u_out, int32_t flags, uint32_t seed, void* stream);
+/* Options of lbm_lattice_run_opts (any field may be zero / NULL).
+ *   step_counter : device int.  When set, step s of the call draws its random
+ *                  bits from (seed + s + *step_counter) read on the device, and
+ *                  a last kernel adds nsteps to *step_counter.  A captured CUDA
+ *                  graph of the call then draws new bits on every replay
+ *                  (the counter holds the step index), where a seed passed by
+ *                  value would repeat them.  Without it, step s uses (seed + s).
+ *   probe_*      : the fused step appends (ux, uy) of node (probe_x, probe_y),
+ *                  the velocity of the post-streaming state it collides, at
+ *                  probe_buf[2 * (*probe_count)++] while the count is below
+ *                  probe_cap: the per-step probe of the reference's drivers
+ *                  (np.linalg.norm(velocity[px, py]) each step, src/experiments.py:690,703-704)
+ *                  without a host round trip.  A probe keeps the boundary sources
+ *                  inside the step (no boundary-node pass), so the node is
+ *                  recorded once per step. */
+typedef struct lbm_run_options {
+  int32_t* step_counter;
+  int32_t probe_x, probe_y, probe_cap;
+  double* probe_buf;
+  int32_t* probe_count;
+} lbm_run_options;
+/* lbm_lattice_run with options; lbm_lattice_run(...) is lbm_lattice_run_opts(..., NULL, stream). */
+int lbm_lattice_run_opts(const lbm_geometry* g, int32_t storage, void* pop_a, void* pop_b, int64_t pitch,
+                         void* aux_a, void* aux_b, double omega, int32_t nsteps, double* rho_out,
+                         double* u_out, int32_t flags, uint32_t seed, const lbm_run_options* opt,
+                         void* stream);
 /* Materialise the current (post-streaming, post-boundary) state in the
  * reference layout: f_out[nx][ny][9], rho_out[nx][ny], u_out[nx][ny][2]
  * (any may be NULL). */

@@ -15,7 +15,7 @@ no CPU path.
 """
 from . import _lib  # noqa: F401
 from . import boundary_conditions, boundary_utils, initial_values, lattice_boltzmann_method  # noqa: F401
-from . import analysis, batch, scenarios, serving  # noqa: F401
+from . import analysis, batch, scenarios, serving, sweeps  # noqa: F401
 from .boundary_utils import Boundary  # noqa: F401
 from .lattice import Lattice  # noqa: F401
 

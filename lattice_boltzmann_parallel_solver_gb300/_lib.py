@@ -60,6 +60,13 @@ class BatchLattice(C.Structure):
                 ("probe_cap", i32), ("probe_buf", vp), ("probe_count", vp), ("seed", C.c_uint32),
                 ("flags", i32), ("rows", i32)]
 
+
+class RunOptions(C.Structure):
+    """lbm_run_options in include/lbm_gb300.h"""
+    _fields_ = [("step_counter", vp), ("probe_x", i32), ("probe_y", i32), ("probe_cap", i32),
+                ("probe_buf", vp), ("probe_count", vp)]
+
+
 # name: (restype, argtypes)
 SIGNATURES = {
     "lbm_version": (C.c_int, []),
@@ -81,6 +88,8 @@ SIGNATURES = {
     "lbm_lattice_pop_bytes": (C.c_size_t, [i32, i32, i64, i32]),
     "lbm_lattice_init": (C.c_int, [GP, i32, vp, vp, vp, f64, vp, i64, vp, i32, vp]),
     "lbm_lattice_run": (C.c_int, [GP, i32, vp, vp, i64, vp, vp, f64, i32, vp, vp, i32, C.c_uint32, vp]),
+    "lbm_lattice_run_opts": (C.c_int, [GP, i32, vp, vp, i64, vp, vp, f64, i32, vp, vp, i32, C.c_uint32,
+                                       C.POINTER(RunOptions), vp]),
     "lbm_lattice_read": (C.c_int, [GP, i32, vp, i64, vp, vp, vp, vp, vp]),
     "lbm_reduce_scratch_bytes": (C.c_size_t, [i64]),
     "lbm_reduce_moments_f64": (C.c_int, [vp, i64, vp, C.c_size_t, vp, vp]),

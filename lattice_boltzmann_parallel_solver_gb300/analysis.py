@@ -34,13 +34,54 @@ def mass_momentum(f) -> tuple:
     return m, px, py
 
 
-def strouhal(trace, length: float, velocity: float, start: int = 0) -> float:
-    """St = f L / u with f = |fftfreq[argmax |FFT(trace - mean)|]| in float64 on the
-    device (visualizations_utils.py:157-167)."""
-    t = torch.as_tensor(trace, dtype=torch.float64, device="cuda")[start:]
+def _as_trace(trace, device=None):
+    if isinstance(trace, torch.Tensor):
+        return trace.to(dtype=torch.float64, device=device or trace.device)
+    return torch.as_tensor(np.asarray(trace, dtype=np.float64), device=device or "cpu")
+
+
+def strouhal(trace, length: float, velocity: float, start: int = 0, method: str = "argmax",
+             device=None) -> float:
+    """St = f L / u of the dominant frequency f (cycles per time step) of trace[start:].
+
+    method "argmax": f = |fftfreq[argmax |FFT(trace - mean)|]|, the reference's
+    definition (visualizations_utils.py:157-167), resolved to one FFT bin
+    (1 / len cycles per step).  method "interp": spectral_peak's sub-bin
+    estimate.  Float64, on ``device`` (default: where the trace is; NumPy input
+    on the host)."""
+    t = _as_trace(trace, device)[start:]
+    if method == "interp":
+        return spectral_peak(t)[0] * length / velocity
+    assert method == "argmax", "method is 'argmax' or 'interp'"
     spec = torch.fft.fft(t - t.mean()).abs()
     freq = torch.fft.fftfreq(t.numel(), 1.0, dtype=torch.float64, device=t.device)
     return float(freq[int(torch.argmax(spec))].abs()) * length / velocity
+
+
+def spectral_peak(trace, start: int = 0, pad: int = 16, device=None) -> tuple:
+    """Sub-bin frequency of the largest spectral peak of trace[start:], in cycles
+    per sample: the mean is removed, a (symmetric) Hann window applied, the FFT
+    zero-padded to ``pad`` times the length, and a Gaussian interpolation -- a
+    parabola through the logarithms of the peak bin and its two neighbours --
+    places the peak between bins (M. Gasior, J. L. Gonzalez, "Improving FFT
+    frequency measurement resolution by parabolic and Gaussian spectrum
+    interpolation", 2004).  Bins below 2 (unpadded) are left out,
+    the remains of the mean.  Returns (frequency, bin, padded bin): the bin width
+    1/len that the argmax estimate is quantised to, and 1/(pad len); the
+    interpolation places the peak to a small fraction of the padded bin."""
+    t = _as_trace(trace, device)[start:]
+    n = t.numel()
+    assert n >= 8, "trace too short"
+    x = (t - t.mean()) * torch.hann_window(n, periodic=False, dtype=torch.float64, device=t.device)
+    m = pad * n
+    spec = torch.fft.rfft(x, n=m).abs()
+    lo = 2 * pad
+    k = lo + int(torch.argmax(spec[lo:]))
+    k = min(k, spec.numel() - 2)
+    a, b, c = torch.log(spec[k - 1:k + 2].clamp_min(1e-300)).tolist()
+    den = a - 2.0 * b + c
+    p = 0.5 * (a - c) / den if den != 0.0 else 0.0
+    return (k + p) / m, 1.0 / n, 1.0 / m
 
 
 def fit_decay_viscosity(amplitudes, times, eps: float, wavelength: float, iters: int = 50) -> float:

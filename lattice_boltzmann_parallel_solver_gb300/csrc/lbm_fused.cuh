@@ -58,9 +58,17 @@ struct KParams {
   // seed per step
   uint32_t seed;
   int sr;
+  // optional device step counter: when set, a launch's random bits come from
+  // hash32(seed + *step_dev) (seed then holds the unhashed base + step index),
+  // so a captured CUDA graph of steps draws new bits on every replay
+  const int32_t* step_dev;
   // fixed-point storage: constants of its collision
   fx::QConsts qc;
 };
+
+__device__ __forceinline__ uint32_t launch_seed(const KParams& P) {
+  return P.step_dev != nullptr ? hash32(P.seed + (uint32_t)__ldg(P.step_dev)) : P.seed;
+}
 
 // skip_bc: a body without its boundary block leaves the probe of a node that
 // the batched boundary-node pass recomputes (a listed boundary node or, under

@@ -186,7 +186,8 @@ __global__ void __launch_bounds__(THREADS, (STORE == LBM_STORE_F16S || STORE == 
                                                : 1)
     fused_v2_kernel(const __grid_constant__ KParams P) {
   fused_v2_body<STORE, NPT, HAS_BC, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out,
-                                                  (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y, P.seed);
+                                                  (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y,
+                                                  launch_seed(P));
 }
 
 // one node per thread: registers capped so that 1024 threads fit on an SM
@@ -209,8 +210,12 @@ __global__ void __launch_bounds__(THREADS) fixup_v2_kernel(const __grid_constant
   if constexpr (STORE == LBM_STORE_FX64)
     fused_fx_body<1, true, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out, x, y);
   else
-    fused_v2_body<STORE, 1, true, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out, x, y, P.seed);
+    fused_v2_body<STORE, 1, true, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out, x, y,
+                                                launch_seed(P));
 }
+
+// adds the steps of a lbm_lattice_run_opts call to its device step counter
+__global__ void advance_counter_kernel(int32_t* counter, int32_t n) { *counter += n; }
 
 // ---------------------------------------------------------------------------
 // host side
@@ -334,7 +339,9 @@ static int64_t split_nodes(int storage) {
 static int launch_fused(int storage, int flags, const KParams& P, cudaStream_t s) {
   const int npt = v2_npt(storage, flags, P);
   const int64_t nodes = (int64_t)P.g.nx * P.g.ny;
+  // a probe keeps the sources inside the step, so its node is recorded once
   const bool split = npt > 0 && !(flags & LBM_FLAG_BC_INLINE) && P.g.bcmask != nullptr && P.g.n_bcnodes > 0 &&
+                     P.probe_buf == nullptr &&
                      (nodes >= split_nodes(storage) || (flags & LBM_FLAG_BC_SPLIT)) &&
                      (int64_t)P.g.n_bcnodes * 8 <= nodes;
   if (!split) return launch_fused_step(storage, npt, flags, P, s);
@@ -426,6 +433,14 @@ int lbm_lattice_init(const lbm_geometry* g, int32_t storage, const double* f, co
 int lbm_lattice_run(const lbm_geometry* g, int32_t storage, void* pop_a, void* pop_b, int64_t pitch,
                     void* aux_a, void* aux_b, double omega, int32_t nsteps, double* rho_out,
                     double* u_out, int32_t flags, uint32_t seed, void* stream) {
+  return lbm_lattice_run_opts(g, storage, pop_a, pop_b, pitch, aux_a, aux_b, omega, nsteps, rho_out, u_out, flags,
+                              seed, nullptr, stream);
+}
+
+int lbm_lattice_run_opts(const lbm_geometry* g, int32_t storage, void* pop_a, void* pop_b, int64_t pitch,
+                         void* aux_a, void* aux_b, double omega, int32_t nsteps, double* rho_out,
+                         double* u_out, int32_t flags, uint32_t seed, const lbm_run_options* opt,
+                         void* stream) {
   KParams P;
   std::memset(&P, 0, sizeof(P));
   if (!to_geok(g, P.g)) return last_status();
@@ -436,13 +451,28 @@ int lbm_lattice_run(const lbm_geometry* g, int32_t storage, void* pop_a, void* p
   if (g->outlet && (aux_a == nullptr || aux_b == nullptr || aux_a == aux_b))
     return set_error(LBM_ERR_ARG, "the outlet needs two distinct aux buffers");
   if (nsteps < 0) return set_error(LBM_ERR_ARG, "nsteps must be >= 0");
+  P.probe_x = P.probe_y = -1;
+  if (opt != nullptr && opt->probe_buf != nullptr) {
+    if (opt->probe_count == nullptr || opt->probe_cap < 0)
+      return set_error(LBM_ERR_ARG, "a probe needs probe_count and probe_cap >= 0");
+    if (opt->probe_x < 0 || opt->probe_x >= g->nx || opt->probe_y < 0 || opt->probe_y >= g->ny)
+      return set_error(LBM_ERR_ARG, "the probe node lies outside the lattice");
+    P.probe_x = opt->probe_x;
+    P.probe_y = opt->probe_y;
+    P.probe_cap = opt->probe_cap;
+    P.probe_buf = opt->probe_buf;
+    P.probe_count = opt->probe_count;
+  }
+  const int32_t* counter = opt != nullptr ? opt->step_counter : nullptr;
   P.pitch = pitch;
   P.plane = pitch * g->ny;
   P.omega = omega;
   P.sr = (flags & LBM_FLAG_STOCHASTIC) != 0;
   P.qc = fx::q_consts(omega);
+  P.step_dev = counter;
   for (int s = 0; s < nsteps; ++s) {
-    P.seed = hash32(seed + (uint32_t)s);
+    // with a device counter the kernels hash (seed + s + *counter) themselves
+    P.seed = counter != nullptr ? seed + (uint32_t)s : hash32(seed + (uint32_t)s);
     const bool even = (s % 2) == 0;
     P.pop_in = even ? pop_a : pop_b;
     P.pop_out = even ? pop_b : pop_a;
@@ -452,6 +482,11 @@ int lbm_lattice_run(const lbm_geometry* g, int32_t storage, void* pop_a, void* p
     P.rho_out = OutView{last ? rho_out : nullptr, 1, pitch, 0};
     P.u_out = OutView{last ? u_out : nullptr, 1, pitch, pitch * g->ny};
     if (int e = launch_fused(storage, flags, P, (cudaStream_t)stream)) return e;
+  }
+  if (counter != nullptr && nsteps > 0) {
+    advance_counter_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(opt->step_counter, nsteps);
+    count_launch();
+    if (int e = check_launch("advance_counter_kernel")) return e;
   }
   return LBM_OK;
 }

@@ -19,6 +19,8 @@ moments, collides and writes the new post-collision populations once.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import torch
 
@@ -41,7 +43,8 @@ class Lattice:
 
     def __init__(self, nx: int, ny: int, omega: float, boundary=None, storage: str = None,
                  exact: bool = False, device: str = "cuda", generic: bool = False, npt: int = 0,
-                 stochastic: bool = None, seed: int = 0, bc_inline: bool | None = None):
+                 stochastic: bool = None, seed: int = 0, bc_inline: bool | None = None,
+                 probe: tuple = None, probe_cap: int = 0):
         """``generic`` forces the one-node-per-thread kernel; ``npt`` sets the
         nodes per thread of the vectorised kernel (0 = the default for the storage).
         ``stochastic`` (default: on for the 16-bit storages) rounds the stored
@@ -53,7 +56,10 @@ class Lattice:
         the step (same results).  ``bc_inline`` True / False forces the one or
         the other.  The
         default storage is "fx64", or "f64" with ``exact`` (the reference's
-        float64 operation order, bit for bit)."""
+        float64 operation order, bit for bit).  ``probe`` = (x, y) records the
+        velocity of that node at every fused step, up to ``probe_cap`` steps
+        (``probe_trace``): the per-step probe of the reference's drivers
+        (src/experiments.py:690,703-704) kept on the device."""
         A.require_cuda()
         assert 0 < omega < 2
         if storage is None:
@@ -82,6 +88,12 @@ class Lattice:
         self.t = 0
         self._init = None
         self._graphs = {}
+        self._stepdev = None
+        self.probe = None if probe is None else (int(probe[0]), int(probe[1]))
+        if self.probe is not None:
+            assert 0 <= self.probe[0] < self.nx and 0 <= self.probe[1] < self.ny, "probe outside the lattice"
+            self.probe_buf = torch.zeros(2 * max(int(probe_cap), 1), dtype=torch.float64, device=self.device)
+            self.probe_count = torch.zeros(1, dtype=torch.int32, device=self.device)
 
     # -- state ------------------------------------------------------------------
     def set_state(self, f, density=None, velocity=None):
@@ -98,6 +110,8 @@ class Lattice:
         self.t = 0
         self.cur = 0
         self._graphs.clear()
+        if self.probe is not None:
+            self.probe_count.zero_()
         return self
 
     @property
@@ -113,12 +127,25 @@ class Lattice:
         self._init = None
         self.t += 1
 
+    def _options(self, counter=None):
+        """lbm_run_options for the probe and/or a device step counter (None: neither)."""
+        if self.probe is None and counter is None:
+            return None
+        o = _lib.RunOptions()
+        o.step_counter = None if counter is None else counter.data_ptr()
+        o.probe_x, o.probe_y = self.probe if self.probe is not None else (-1, -1)
+        if self.probe is not None:
+            o.probe_cap = self.probe_buf.numel() // 2
+            o.probe_buf, o.probe_count = self.probe_buf.data_ptr(), self.probe_count.data_ptr()
+        return o
+
     def _run(self, n: int, rho_out=None, u_out=None):
         a, b = self.cur, 1 - self.cur
-        _lib.call("lbm_lattice_run", self.geo.ref, self.store_id, self.pop[a].data_ptr(), self.pop[b].data_ptr(),
-                  self.pitch, self.aux[a].data_ptr(), self.aux[b].data_ptr(), self.omega, int(n),
-                  A.ptr(rho_out), A.ptr(u_out), self.flags, (self.seed + self.t - 1) & 0xFFFFFFFF,
-                  A.stream())
+        opts = self._options()
+        _lib.call("lbm_lattice_run_opts", self.geo.ref, self.store_id, self.pop[a].data_ptr(),
+                  self.pop[b].data_ptr(), self.pitch, self.aux[a].data_ptr(), self.aux[b].data_ptr(), self.omega,
+                  int(n), A.ptr(rho_out), A.ptr(u_out), self.flags, (self.seed + self.t - 1) & 0xFFFFFFFF,
+                  None if opts is None else ctypes.byref(opts), A.stream())
         if n % 2:
             self.cur = b
         self.t += n
@@ -137,25 +164,37 @@ class Lattice:
     def step_graph(self, n: int, chunk: int = 64):
         """Advance n steps replaying a captured CUDA graph of ``chunk`` fused
         steps (chunk even, so the buffers return to their places); for small
-        lattices where launch latency would dominate."""
+        lattices where launch latency would dominate.  Results equal step(n)
+        bit for bit: with stochastic rounding the captured steps read the step
+        index from a device counter, so every replay draws the random bits that
+        step() would."""
         assert chunk % 2 == 0 and chunk > 0
         if self._init is not None:
             self._first()
             n -= 1
         full, rest = divmod(max(n, 0), chunk)
         if full:
+            counted = bool(self.flags & _lib.FLAG_STOCHASTIC)
+            if counted:
+                if self._stepdev is None:
+                    self._stepdev = torch.zeros(1, dtype=torch.int32, device=self.device)
+                # the step index the captured launches add to the seed (ordered before the replays)
+                self._stepdev.fill_(self.t - 1)
             key = (chunk, self.cur)
             g = self._graphs.get(key)
             if g is None:
                 g = torch.cuda.CUDAGraph()
                 side = torch.cuda.Stream()
                 side.wait_stream(torch.cuda.current_stream())
+                opts = self._options(self._stepdev if counted else None)
+                seed = self.seed if counted else (self.seed + self.t - 1) & 0xFFFFFFFF
                 with torch.cuda.stream(side):
                     with torch.cuda.graph(g, stream=side):
-                        _lib.call("lbm_lattice_run", self.geo.ref, self.store_id, self.pop[self.cur].data_ptr(),
-                                  self.pop[1 - self.cur].data_ptr(), self.pitch, self.aux[self.cur].data_ptr(),
-                                  self.aux[1 - self.cur].data_ptr(), self.omega, chunk, 0, 0, self.flags,
-                                  (self.seed + self.t - 1) & 0xFFFFFFFF, side.cuda_stream)
+                        _lib.call("lbm_lattice_run_opts", self.geo.ref, self.store_id,
+                                  self.pop[self.cur].data_ptr(), self.pop[1 - self.cur].data_ptr(), self.pitch,
+                                  self.aux[self.cur].data_ptr(), self.aux[1 - self.cur].data_ptr(), self.omega,
+                                  chunk, 0, 0, self.flags, seed, None if opts is None else ctypes.byref(opts),
+                                  side.cuda_stream)
                 torch.cuda.current_stream().wait_stream(side)
                 self._graphs[key] = g
             for _ in range(full):
@@ -164,6 +203,14 @@ class Lattice:
         if rest:
             self._run(rest)
         return self
+
+    def probe_trace(self) -> torch.Tensor:
+        """(ux, uy) recorded at the probe node, one row per fused step: row k is the
+        velocity of the state after k + 1 steps (the first step only collides
+        the initial state; the velocity after the last step is read())."""
+        assert self.probe is not None, "the lattice has no probe"
+        n = min(int(self.probe_count.item()), self.probe_buf.numel() // 2)
+        return self.probe_buf[: 2 * n].view(n, 2)
 
     # -- read-out ---------------------------------------------------------------
     def read(self, want_f: bool = True):

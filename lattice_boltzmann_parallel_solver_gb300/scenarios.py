@@ -34,21 +34,29 @@ def cavity(n, u_lid=0.1):
     return equilibrium_np(rho, u), rho, u, BU.cavity_boundary_conditions(n, n, u_lid, 1.0)
 
 
-def von_karman(lx=420, ly=180, plate=40, re=100.0, u_in=0.1, noise=1e-3, seed=0, plate_offset=1,
-               walls=True, plate_x=None):
-    """Channel with a flat plate (config-3 form): inlet (u_in, 0), the reference's
-    outlet, top/bottom bounce-back, plate of ``plate`` rows at x = lx//4 shifted by
-    ``plate_offset`` rows, nu = u_in * plate / re, seeded U(-noise, noise) on u_y."""
+def von_karman_start(lx, ly, u_in=0.1, noise=1e-3, seed=0):
+    """Start of the channel study: rho = 1, u = (u_in, U(-noise, noise)) with u_y
+    drawn by numpy.random.default_rng(seed), f = f_eq(rho, u)."""
     rng = np.random.default_rng(seed)
-    nu = u_in * plate / re
-    omega = 1.0 / (3.0 * nu + 0.5)
     rho = np.ones((lx, ly))
     u = np.zeros((lx, ly, 2))
     u[..., 0] = u_in
     u[..., 1] = rng.uniform(-noise, noise, (lx, ly))
+    return equilibrium_np(rho, u), rho, u
+
+
+def von_karman(lx=420, ly=180, plate=40, re=100.0, u_in=0.1, noise=1e-3, seed=0, plate_offset=1,
+               walls=True, plate_x=None):
+    """Channel with a flat plate (the precision study's form): inlet (u_in, 0), the
+    reference's outlet, top/bottom bounce-back, plate of ``plate`` rows at x = lx//4
+    shifted by ``plate_offset`` rows, nu = u_in * plate / re, seeded U(-noise, noise)
+    on u_y."""
+    nu = u_in * plate / re
+    omega = 1.0 / (3.0 * nu + 0.5)
+    f, rho, u = von_karman_start(lx, ly, u_in, noise, seed)
     bnd = BU.von_karman_boundary_conditions(lx, ly, 1.0, u_in, plate, plate_x=plate_x, walls=walls,
                                             plate_offset=plate_offset)
-    return equilibrium_np(rho, u), rho, u, omega, bnd
+    return f, rho, u, omega, bnd
 
 
 def batch_sweep_params(n=256, seed=2024):

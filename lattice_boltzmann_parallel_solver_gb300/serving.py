@@ -39,6 +39,7 @@ class Request:
     u0: np.ndarray
     arrival: float = 0.0          # seconds after the stream starts
     params: dict = field(default_factory=dict)
+    init: object = None           # () -> (f0, rho0, u0): the initial state built on demand
     # filled in by the engine
     admitted: float = None
     finished: float = None
@@ -53,12 +54,30 @@ class Request:
     def nodes(self):
         return self.nx * self.ny
 
+    def initial_state(self):
+        """(f0, rho0, u0): the given arrays, else built by ``init``."""
+        if self.f0 is not None:
+            return self.f0, self.rho0, self.u0
+        return self.init()
 
-def request_mix(n, rate=50.0, seed=7, step_range=(1000, 50000), kinds=("couette", "poiseuille", "von_karman")):
+
+def _rest_state(nx, ny, device="cuda"):
+    """rho = 1, u = 0 and its equilibrium (the weights) on the device."""
+    w = torch.tensor([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4, dtype=torch.float64, device=device)
+    return (w.expand(nx, ny, 9).contiguous(), torch.ones((nx, ny), dtype=torch.float64, device=device),
+            torch.zeros((nx, ny, 2), dtype=torch.float64, device=device))
+
+
+def request_mix(n, rate=50.0, seed=7, step_range=(1000, 50000), kinds=("couette", "poiseuille", "von_karman"),
+                lazy=False):
     """Seeded Poisson arrivals (mean ``rate`` per second) of mixed requests:
     Couette (moving top wall u_w in [0.01, 0.1], ny in [32, 512], nx = ny),
     pressure-driven Poiseuille (delta rho log-uniform in [1e-4, 1e-2], nx x ny
-    up to 2048 x 512) and the von Karman channel (420 x 180, Re 100)."""
+    up to 2048 x 512) and the von Karman channel (420 x 180, Re 100).  The
+    arrival gaps are rate-scaled draws of one seeded stream, so the same seed
+    gives the same requests (kinds, sizes, budgets) at every rate.  With ``lazy``
+    the initial states are built on the device at admission (long streams
+    would not fit the host memory up front)."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
@@ -70,21 +89,25 @@ def request_mix(n, rate=50.0, seed=7, step_range=(1000, 50000), kinds=("couette"
             ny = int(rng.integers(32, 513))
             nx = ny
             uw = float(rng.uniform(0.01, 0.1))
-            rho, u = np.ones((nx, ny)), np.zeros((nx, ny, 2))
             bnd = BU.Boundary([BU.rigid_wall(_row(nx, ny, 0)),
                                BU.moving_wall(_row(nx, ny, -1), np.array([uw, 0.0]), 1.0)])
-            req = Request(rid, kind, nx, ny, 1.0, steps, bnd, S.equilibrium_np(rho, u), rho, u, t, {"u_w": uw})
+            req = Request(rid, kind, nx, ny, 1.0, steps, bnd, None, None, None, t, {"u_w": uw},
+                          init=lambda nx=nx, ny=ny: _rest_state(nx, ny))
         elif kind == "poiseuille":
             nx = int(rng.integers(64, 2049))
             ny = int(rng.integers(16, 513))
             drho = float(math.exp(rng.uniform(math.log(1e-4), math.log(1e-2))))
             p_in, p_out = (1 + drho / 2) / 3, (1 - drho / 2) / 3
-            rho, u = np.ones((nx, ny)), np.zeros((nx, ny, 2))
             bnd = BU.poiseuille_flow_boundary_conditions(nx, ny, p_in, p_out)
-            req = Request(rid, kind, nx, ny, 1.5, steps, bnd, S.equilibrium_np(rho, u), rho, u, t, {"drho": drho})
+            req = Request(rid, kind, nx, ny, 1.5, steps, bnd, None, None, None, t, {"drho": drho},
+                          init=lambda nx=nx, ny=ny: _rest_state(nx, ny))
         else:
-            f, rho, u, om, bnd = S.von_karman(420, 180, plate=40, re=100, seed=rid)
-            req = Request(rid, kind, 420, 180, om, steps, bnd, f, rho, u, t, {"re": 100})
+            om = 1.0 / (3.0 * (0.1 * 40 / 100.0) + 0.5)
+            bnd = BU.von_karman_boundary_conditions(420, 180, 1.0, 0.1, 40, walls=True, plate_offset=1)
+            req = Request(rid, kind, 420, 180, om, steps, bnd, None, None, None, t, {"re": 100},
+                          init=lambda rid=rid: S.von_karman_start(420, 180, 0.1, 1e-3, seed=rid))
+        if not lazy:
+            req.f0, req.rho0, req.u0 = req.init()
         out.append(req)
     return out
 
@@ -138,7 +161,11 @@ class ServingEngine:
                     self.used + self.state_bytes(waiting[0]) <= self.hbm_budget:
                 r = waiting.pop(0)
                 r.admitted = now
-                m = b.add(Member(r.nx, r.ny, r.omega, r.boundary, steps=r.steps, f0=r.f0, rho0=r.rho0, u0=r.u0))
+                f0, rho0, u0 = r.initial_state()
+                m = b.add(Member(r.nx, r.ny, r.omega, r.boundary, steps=r.steps, f0=f0, rho0=rho0, u0=u0))
+                # the first step has consumed the initial state
+                m.f0 = m.rho0 = m.u0 = None
+                del f0, rho0, u0
                 self.live.append((r, m))
                 self.used += self.state_bytes(r)
             if not self.live:

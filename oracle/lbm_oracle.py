@@ -300,12 +300,21 @@ def plate_rows(ly, plate_size):
     return y_min, y_max, ly // 2 + plate_size // 2 - 1, ly // 2 - plate_size // 2
 
 
-def von_karman_boundary(lx, ly, density_in, velocity_in, plate_size, plate_x=None):
+def von_karman_boundary(lx, ly, density_in, velocity_in, plate_size, plate_x=None, walls=False,
+                        plate_offset=0):
     """Inlet, outlet, thin plate left/right faces and corners on an unpadded
-    periodic domain; the single-rank interior of boundary_utils.py:113-205."""
+    periodic domain; the single-rank interior of boundary_utils.py:113-205.
+
+    The channel form of the von Karman study (no reference composition exists
+    for it) adds, after the plate, a rigid bottom row and a rigid top row
+    through the reference's rigid_wall closure (boundary_conditions.py:78-113;
+    a y-wall mask picks directions 4,7,8 at y=0 and 2,5,6 at y=ly-1,
+    :18-27), with ``walls=True``; ``plate_offset`` moves the plate's rows by that
+    many nodes (rows 71..110 instead of 70..109 at ly=180 for +1)."""
     px = lx // 4 if plate_x is None else plate_x
-    y_min, y_max, y_up, y_lo = plate_rows(ly, plate_size)
+    y_min, y_max, y_up, y_lo = (r + plate_offset for r in plate_rows(ly, plate_size))
     feq_in = inlet_populations((1, ly), density_in, velocity_in)[0]
+    wall_bcs = [rigid_wall(_row_mask(lx, ly, 0)), rigid_wall(_row_mask(lx, ly, -1))] if walls else []
 
     def boundary(f_pre, f_post, rho=None, u=None, f_prev=None):
         f_post[0, :, :] = feq_in
@@ -319,6 +328,8 @@ def von_karman_boundary(lx, ly, density_in, velocity_in, plate_size, plate_x=Non
             f_post[px + 1, y_min:y_max, a] = f_pre[px + 1, y_min:y_max, b]
         f_post[px + 1, y_up, [1, 5]] = f_pre[px + 1, y_up, [3, 7]]
         f_post[px + 1, y_lo, [1, 8]] = f_pre[px + 1, y_lo, [3, 6]]
+        for wall in wall_bcs:
+            f_post = wall(f_pre, f_post)
         return f_post
     return boundary
 
@@ -361,6 +372,20 @@ def cavity_boundary(n_x, n_y, u_lid=0.1, avg_density=1.0):
         f_post = bottom(f_pre, f_post)
         return lid(f_pre, f_post)
     return boundary
+
+
+def von_karman_channel_start(lx, ly, velocity_in, noise, seed):
+    """Start of the channel form: rho = 1, u = (velocity_in, U(-noise, noise)) with
+    the u_y field drawn by numpy.random.default_rng(seed).uniform over (lx, ly),
+    f = f_eq(rho, u) (the reference's initial value
+    density_1_velocity_x_u0_velocity_y_0_initial, initial_values.py:109-123,
+    with the seeded transverse perturbation that breaks the symmetry)."""
+    rng = np.random.default_rng(seed)
+    rho = np.ones((lx, ly))
+    u = np.zeros((lx, ly, 2))
+    u[..., 0] = velocity_in
+    u[..., 1] = rng.uniform(-noise, noise, (lx, ly))
+    return equilibrium(rho, u), rho, u
 
 
 # ---------------------------------------------------------------------------

@@ -3,7 +3,7 @@
 Run from the repository root in a container where the reference checkout is
 available (it is read, never modified):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the reference checkout>
 
 The reference is pure Python/NumPy.  Its ``boundary_utils`` and
 ``parallelization_utils`` modules import ``mpi4py``; a single-rank stand-in
@@ -253,4 +253,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the reference checkout>")
+    main(sys.argv[1])

@@ -57,33 +57,53 @@ def test_argument_errors_without_gpu(lib):
 
 
 @pytest.mark.skipif(shutil.which("gcc") is None, reason="gcc not available")
-def test_geometry_struct_layout_matches_c(tmp_path):
-    src = tmp_path / "layout.c"
-    fields = [f[0] for f in _lib.Geometry._fields_]
-    body = "".join('printf("%s %%zu\\n", offsetof(lbm_geometry, %s));' % (n, n) for n in fields)
+@pytest.mark.parametrize("cname,pyname", [("lbm_geometry", "Geometry"), ("lbm_batch_lattice", "BatchLattice"),
+                                          ("lbm_run_options", "RunOptions")])
+def test_struct_layout_matches_c(tmp_path, cname, pyname):
+    cls = getattr(_lib, pyname)
+    src = tmp_path / ("%s.c" % cname)
+    fields = [f[0] for f in cls._fields_]
+    body = "".join('printf("%s %%zu\\n", offsetof(%s, %s));' % (n, cname, n) for n in fields)
     src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "lbm_gb300.h"\n'
-                   'int main(void){printf("size %%zu\\n", sizeof(lbm_geometry));%s return 0;}\n' % body)
-    exe = tmp_path / "layout"
+                   'int main(void){printf("size %%zu\\n", sizeof(%s));%s return 0;}\n' % (cname, body))
+    exe = tmp_path / cname
     subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
     out = dict(line.split() for line in subprocess.check_output([str(exe)]).decode().splitlines())
-    assert int(out["size"]) == ctypes.sizeof(_lib.Geometry)
+    assert int(out["size"]) == ctypes.sizeof(cls)
     for n in fields:
-        assert int(out[n]) == getattr(_lib.Geometry, n).offset, n
+        assert int(out[n]) == getattr(cls, n).offset, n
 
 
-@pytest.mark.skipif(shutil.which("gcc") is None, reason="gcc not available")
-def test_batch_lattice_struct_layout_matches_c(tmp_path):
-    src = tmp_path / "batch_layout.c"
-    fields = [f[0] for f in _lib.BatchLattice._fields_]
-    body = "".join('printf("%s %%zu\\n", offsetof(lbm_batch_lattice, %s));' % (n, n) for n in fields)
-    src.write_text('#include <stdio.h>\n#include <stddef.h>\n#include "lbm_gb300.h"\n'
-                   'int main(void){printf("size %%zu\\n", sizeof(lbm_batch_lattice));%s return 0;}\n' % body)
-    exe = tmp_path / "batch_layout"
-    subprocess.check_call(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
-    out = dict(line.split() for line in subprocess.check_output([str(exe)]).decode().splitlines())
-    assert int(out["size"]) == ctypes.sizeof(_lib.BatchLattice)
-    for n in fields:
-        assert int(out[n]) == getattr(_lib.BatchLattice, n).offset, n
+def test_integration_stub_geometry_matches_binding():
+    """The ctypes stub a maintainer copies from INTEGRATION.md has the binding's
+    fields, sizes and offsets (so the documented struct cannot drift)."""
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    m = re.search(r"```python\n(import ctypes as C\n.*?)```", text, re.S)
+    assert m, "no ctypes stub in INTEGRATION.md"
+    code = m.group(1).replace('lib = C.CDLL("liblbm_gb300.so")', "lib = None")
+    code = code[:code.index("lib.lbm_step_f64.argtypes")]
+    ns = {}
+    exec(compile(code, "INTEGRATION.md", "exec"), ns)
+    stub = ns["Geometry"]
+    assert [f[0] for f in stub._fields_] == [f[0] for f in _lib.Geometry._fields_]
+    assert ctypes.sizeof(stub) == ctypes.sizeof(_lib.Geometry)
+    for name, _ in _lib.Geometry._fields_:
+        assert getattr(stub, name).offset == getattr(_lib.Geometry, name).offset, name
+
+
+def test_run_options_argument_errors_without_gpu(lib):
+    g = _lib.Geometry()
+    g.nx, g.ny = 8, 4
+    o = _lib.RunOptions()
+    o.probe_buf, o.probe_count, o.probe_cap = 4096, 8192, 10
+    o.probe_x, o.probe_y = 8, 0
+    with pytest.raises(AssertionError, match="probe"):
+        _lib.check(lib.lbm_lattice_run_opts(ctypes.byref(g), 0, 1, 2, 32, None, None, 1.0, 1, None, None, 0, 0,
+                                            ctypes.byref(o), None))
+    o.probe_x, o.probe_count = 0, None
+    with pytest.raises(AssertionError, match="probe_count"):
+        _lib.check(lib.lbm_lattice_run_opts(ctypes.byref(g), 0, 1, 2, 32, None, None, 1.0, 1, None, None, 0, 0,
+                                            ctypes.byref(o), None))
 
 
 def test_batch_argument_errors_without_gpu(lib):

@@ -168,3 +168,18 @@ def test_boundary_node_list_matches_the_mask(name):
     got = g.bcnodes.cpu().numpy()
     assert got.dtype == np.int32 and np.array_equal(got, want)
     assert g.struct.n_bcnodes == want.size and 0 < want.size * 8 <= lx * ly
+
+
+@pytest.mark.parametrize("offset", [0, 1])
+def test_von_karman_channel_form(offset):
+    """The channel form (rigid bottom/top rows after the plate, plate moved by
+    ``offset`` rows) compiles to the oracle's composition of the reference's
+    closures, corners included."""
+    lx, ly, d = 84, 36, 8
+    feq_in = O.inlet_populations((1, 1), 1.0, 0.1)[0, 0]
+    pre, post, prev = rand3((lx, ly), 7 + offset)
+    b = BU.Boundary(BU._vk_closures(lx, ly, 1.0, 0.1, d, feq_in=feq_in, walls=True, plate_offset=offset))
+    got = apply_descriptor(compiled(b, lx, ly), pre, post, prev)
+    want = O.von_karman_boundary(lx, ly, 1.0, 0.1, d, walls=True, plate_offset=offset)(pre, post.copy(), None,
+                                                                                         None, prev)
+    assert np.array_equal(got, want)

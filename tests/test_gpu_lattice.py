@@ -91,6 +91,41 @@ def test_graph_replay_matches_launches(pkg):
     assert torch.equal(a.read()[0], b.read()[0])
 
 
+@pytest.mark.parametrize("storage", ["f16", "bf16"])
+def test_graph_replay_matches_launches_stochastic(pkg, storage):
+    """With stochastic rounding the captured steps take their step index from a
+    device counter: graph replays draw the same random bits as plain launches
+    (bit-identical states and probe traces), and consecutive chunks differ."""
+    nx, ny, om, f, rho, u, obnd, pbnd = scenario("vk")
+    a = pkg.Lattice(nx, ny, om, pbnd(), storage=storage, probe=(60, 18), probe_cap=400)
+    a.set_state(f, rho, u).step(301)
+    b = pkg.Lattice(nx, ny, om, pbnd(), storage=storage, probe=(60, 18), probe_cap=400)
+    b.set_state(f, rho, u).step_graph(130, chunk=64).step(7).step_graph(164, chunk=64)
+    assert a.t == b.t == 301
+    assert torch.equal(a.read()[0], b.read()[0])
+    assert torch.equal(a.probe_trace(), b.probe_trace()) and a.probe_trace().shape == (300, 2)
+    # two replays of one captured 64-step chunk equal 128 plain steps: the second
+    # replay draws the bits of steps 65..128, not those of steps 1..64 again
+    c = pkg.Lattice(nx, ny, om, pbnd(), storage=storage).set_state(f, rho, u).step_graph(129, chunk=64)
+    d = pkg.Lattice(nx, ny, om, pbnd(), storage=storage).set_state(f, rho, u).step(129)
+    assert torch.equal(c.read()[0], d.read()[0])
+
+
+def test_probe_records_every_step(pkg):
+    nx, ny, om, f, rho, u, obnd, pbnd = scenario("vk")
+    lat = pkg.Lattice(nx, ny, om, pbnd(), storage="f64", exact=True, probe=(63, 18), probe_cap=50)
+    lat.set_state(f, rho, u)
+    state = (f, rho, u)
+    lat.step(12)
+    tr = lat.probe_trace().cpu().numpy()
+    assert tr.shape == (11, 2)
+    for k in range(11):
+        state = O.step(*state, om, obnd)
+        assert np.array_equal(tr[k], state[2][63, 18]), k
+    with pytest.raises(AssertionError):
+        pkg.Lattice(nx, ny, om, pbnd(), probe=(nx, 0))
+
+
 @pytest.mark.parametrize("shape", [(1, 1), (2, 3), (3, 3), (8, 5), (33, 7), (129, 4), (5, 130)])
 def test_edge_sizes_periodic(pkg, shape):
     nx, ny = shape

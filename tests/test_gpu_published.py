@@ -1,0 +1,194 @@
+"""The reference's published long runs, reproduced on the GPU.
+
+The reference ships the outputs of its own runs (extracted into
+tests/golden/published_physics.npz by tests/golden/make_published.py):
+
+* von Karman at Re 100, 420x180 (src/milestoneQuickFunctionCalls.py:294-341
+  serially for 100 000 steps, src/experiments.py:650-704 over MPI ranks for
+  200 000 steps; the two runs agree bit for bit, their |u| probe traces to
+  one unit in the last place).  The exact float64 form reproduces the final
+  velocity and density fields of the serial run bit for bit (SHA-256 of the
+  raw bytes) and both probe traces to within 2 units in the last place;
+  the fixed-point (fx64) and 16-bit storages reproduce the Strouhal number
+  of the published trace within 1 % by a sub-bin estimate resolved to
+  better than 0.2 %.
+* Couette flow, 20x30, U 0.05, 5000 steps: the linear-regression slope,
+  intercept and r of the published profile (src/experiments.py:304-363).
+* Poiseuille flow, 200x60, omega 1.5, dp 1e-3, 40 000 steps: the published
+  inlet and middle flux areas, their ratio and the quadratic fit
+  (src/experiments.py:377-492).
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import lbm_oracle as O
+
+pytestmark = pytest.mark.gpu
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def pub():
+    with np.load(os.path.join(ROOT, "tests", "golden", "published_physics.npz")) as z:
+        return {k: z[k] for k in z.files}
+
+
+@pytest.fixture(scope="module")
+def pkg():
+    import lattice_boltzmann_parallel_solver_gb300 as P
+    P._lib.load()
+    return P
+
+
+LX, LY, PLATE = 420, 180, 40
+PROBE = (3 * LX // 4, LY // 2)          # experiments.py:674
+
+
+def vk_lattice(pkg, storage, exact=False, cap=200000, **kw):
+    """The reference-mode von Karman run of x_strouhal (y-periodic, plate rows
+    70..109 at x = 105, inlet (1, (0.1, 0)), outlet, nu = 0.04) with a probe at
+    (315, 90)."""
+    omega = np.reciprocal(3 * 0.04 + 0.5)                       # experiments.py:671
+    rho, u = O.density_1_velocity_u0((LX, LY), 0.1)
+    f = O.equilibrium(rho, u)
+    bnd = pkg.boundary_utils.von_karman_boundary_conditions(LX, LY, 1.0, 0.1, PLATE)
+    lat = pkg.Lattice(LX, LY, omega, bnd, storage=storage, exact=exact, probe=PROBE, probe_cap=cap, **kw)
+    return lat.set_state(f, rho, u)
+
+
+def norm_trace(lat):
+    """|u| at the probe after 0, 1, ..., t steps (the reference's vel_at_p)."""
+    uv = lat.probe_trace().cpu().numpy()
+    last = lat.read(want_f=False)[2][PROBE[0], PROBE[1]].cpu().numpy()
+    uv = np.concatenate([uv, last[None, :]], 0)
+    return np.concatenate([[0.1], np.sqrt(uv[:, 0] * uv[:, 0] + uv[:, 1] * uv[:, 1])])
+
+
+def sha256_of(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
+
+
+def ulps(a, b):
+    return float((np.abs(np.asarray(a) - np.asarray(b)) / np.spacing(np.abs(np.asarray(b)))).max())
+
+
+def test_vk_exact_reproduces_published_runs(pkg, pub):
+    from lattice_boltzmann_parallel_solver_gb300 import analysis
+    lat = vk_lattice(pkg, "f64", exact=True)
+    lat.step(100000)
+    _, rho, u = (t.cpu().numpy() if t is not None else None for t in lat.read(want_f=False))
+    # the serial run's final fields (milestoneQuickFunctionCalls.py:338-341), bit for bit
+    assert np.array_equal(u[::7, ::7], pub["vk_serial_velocity_every7"])
+    assert np.array_equal(rho[::7, ::7], pub["vk_serial_density_every7"])
+    assert sha256_of(u) == str(pub["vk_serial_velocity_sha256"])
+    assert sha256_of(rho) == str(pub["vk_serial_density_sha256"])
+    tr = norm_trace(lat)
+    assert tr.shape == (100001,)
+    assert ulps(tr[::50], pub["vk_serial_trace_every50"]) <= 2
+    assert abs(tr.sum() - pub["vk_serial_trace_sum"]) <= 1e-13 * pub["vk_serial_trace_sum"]
+    # on to the 200 000 steps of x_strouhal's trace (experiments.py:700-704)
+    lat.step(100000)
+    tr = norm_trace(lat)
+    assert tr.shape == (200001,)
+    assert ulps(tr[::50], pub["vk100_trace_every50"]) <= 2
+    assert abs(tr.sum() - pub["vk100_trace_sum"]) <= 1e-13 * pub["vk100_trace_sum"]
+    assert abs((tr * tr).sum() - pub["vk100_trace_sumsq"]) <= 1e-13 * pub["vk100_trace_sumsq"]
+    # the reference's post-processing of the same samples gives its number
+    assert analysis.strouhal(tr, 40, 0.1, start=70000) == pytest.approx(float(pub["vk100_st_argmax"]), rel=1e-12)
+    st = analysis.strouhal(tr, 40, 0.1, start=70000, method="interp")
+    assert st == pytest.approx(float(pub["vk100_st_interp"]), rel=1e-9)
+
+
+@pytest.mark.parametrize("storage", ["fx64", "f16", "bf16", "f32"])
+def test_vk_strouhal_within_one_percent(pkg, pub, storage):
+    """Strouhal number of the 200 000-step |u| trace after step 70 000 against the
+    published trace, by the sub-bin estimate (resolution: the padded bin is
+    1/(16 x 130 001) cycles per step, 0.01 % of St; the reference's own argmax is
+    quantised to 0.68 %)."""
+    from lattice_boltzmann_parallel_solver_gb300 import analysis
+    lat = vk_lattice(pkg, storage)
+    lat.step(200000)
+    tr = norm_trace(lat)
+    f, b, pb = analysis.spectral_peak(tr, start=70000)
+    st = f * 40 / 0.1
+    assert pb * 40 / 0.1 / st < 2e-3
+    err = abs(st - float(pub["vk100_st_interp"])) / float(pub["vk100_st_interp"])
+    print("%s: St %.6f against published %.6f (%.3e), trace max |diff| %.3e" % (
+        storage, st, float(pub["vk100_st_interp"]), err,
+        np.abs(tr[::50] - pub["vk100_trace_every50"]).max()))
+    assert err <= 0.01
+
+
+def test_reynolds_sweep_against_published(pkg, pub):
+    """The Reynolds sweep of src/main.py:150-177 (Re 40 ... 200, 200 000 steps each)
+    as one batch in fx64: each point's Strouhal number by the reference's
+    post-processing lands within one FFT bin of the published one, and by the
+    sub-bin estimate within 1 %."""
+    from lattice_boltzmann_parallel_solver_gb300 import sweeps
+    res = sweeps.strouhal_sweep("reynolds", steps=200000, storage="fx64")
+    assert [r["label"] for r in res] == list(pub["re_sweep_re"])
+    for r, st_a, st_i in zip(res, pub["re_sweep_st_argmax"], pub["re_sweep_st_interp"]):
+        assert r["start"] in pub["re_sweep_start"]
+        print("Re %d: St %.5f (published %.5f), argmax %.5f (published %.5f, bin %.5f)" % (
+            r["label"], r["strouhal"], st_i, r["strouhal_argmax"], st_a, r["strouhal_bin"]))
+        assert abs(r["strouhal_argmax"] - st_a) <= 1.01 * r["strouhal_bin"]
+        assert abs(r["strouhal"] - st_i) <= 0.01 * st_i
+
+
+def couette(pkg, storage, exact=False):
+    # experiments.py:304-325: 20x30, omega 1, U 0.05, rho_avg = mean(rho) = 1, 5000 steps
+    lx, ly = 20, 30
+    rho, u = O.density_1_velocity_0((lx, ly))
+    f = O.equilibrium(rho, u)
+    bnd = pkg.boundary_utils.couette_flow_boundary_conditions(lx, ly, 0.05, np.mean(rho))
+    lat = pkg.Lattice(lx, ly, 1.0, bnd, storage=storage, exact=exact).set_state(f, rho, u).step(5000)
+    return lat.read(want_f=False)[2][..., 0].cpu().numpy()
+
+
+@pytest.mark.parametrize("storage,exact,tol", [("f64", True, 1e-12), ("fx64", False, 1e-9), ("f64", False, 1e-9),
+                                               ("f16", False, 2e-3), ("f32", False, 1e-4)])
+def test_couette_published_regression(pkg, pub, storage, exact, tol):
+    from scipy.stats import linregress
+    vx = couette(pkg, storage, exact)
+    fit = linregress(np.arange(30), vx[20 // 2])                 # experiments.py:354-355
+    assert fit.slope == pytest.approx(float(pub["couette_slope"]), rel=tol)
+    assert fit.intercept == pytest.approx(float(pub["couette_intercept"]), rel=tol)
+    assert fit.rvalue == pytest.approx(float(pub["couette_rvalue"]), rel=max(tol, 1e-12))
+
+
+def poiseuille(pkg, storage, exact=False):
+    # experiments.py:377-406: 200x60, omega 1.5, dp 1e-3, 40 000 steps
+    lx, ly = 200, 60
+    delta_rho = 0.001 * 3
+    p_in, p_out = (1 + (delta_rho / 2)) / 3, (1 - (delta_rho / 2)) / 3
+    rho, u = O.density_1_velocity_0((lx, ly))
+    f = O.equilibrium(rho, u)
+    bnd = pkg.boundary_utils.poiseuille_flow_boundary_conditions(lx, ly, p_in, p_out)
+    lat = pkg.Lattice(lx, ly, 1.5, bnd, storage=storage, exact=exact).set_state(f, rho, u).step(40000)
+    return lat.read(want_f=False)[2][..., 0].cpu().numpy()
+
+
+@pytest.mark.parametrize("storage,exact,tol", [("f64", True, 1e-12), ("fx64", False, 1e-9), ("f64", False, 1e-9),
+                                               ("f16", False, 2e-3), ("f32", False, 1e-4)])
+def test_poiseuille_published_flux_and_fit(pkg, pub, storage, exact, tol):
+    from scipy.optimize import curve_fit
+    trapezoid = getattr(np, "trapezoid", None) or np.trapz
+    vx = poiseuille(pkg, storage, exact)
+    inlet = trapezoid(vx[1, :], np.arange(60))                   # experiments.py:431-433
+    middle = trapezoid(vx[100, :], np.arange(60))
+    assert inlet == pytest.approx(float(pub["poiseuille_area_inlet"]), rel=tol)
+    assert middle == pytest.approx(float(pub["poiseuille_area_middle"]), rel=tol)
+    assert inlet / middle == pytest.approx(float(pub["poiseuille_area_ratio"]), rel=tol)
+    popt, _ = curve_fit(lambda y, a, b, c: a * (y ** 2) + b * y + c, np.arange(60), vx[100, :])
+    # the fitted profile against the published one (its coefficients are printed
+    # to 9 significant digits); the float64-accurate forms also coefficient by coefficient
+    y = np.arange(60.0)
+    fit, want = np.polyval(popt, y), np.polyval(pub["poiseuille_popt"], y)
+    assert np.abs(fit - want).max() <= max(tol, 1e-8) * np.abs(want).max()
+    if tol <= 1e-9:
+        assert np.allclose(popt, pub["poiseuille_popt"], rtol=1e-8, atol=0)
