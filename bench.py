@@ -121,18 +121,19 @@ def strouhal_subbin(P, trace, L=40, u=0.1, start=0):
 
 
 def phase_lag(ref, other, period_guess, window):
-    """Lag tau (steps) maximising the correlation of other(t) with ref(t + tau)
-    over the last ``window`` samples, |tau| <= half a period."""
+    """Lag tau (steps, |tau| <= half a period) maximising the correlation of
+    other(t) with ref(t + tau) over the ``window`` samples that end half a
+    period before the end of the traces (so that every shifted window of ref
+    lies inside it)."""
     ref = np.asarray(ref, dtype=np.float64)
     other = np.asarray(other, dtype=np.float64)
     half = int(period_guess // 2)
-    a = other[-window:] - other[-window:].mean()
+    end = min(len(ref), len(other)) - half
+    a = other[end - window:end] - other[end - window:end].mean()
     best, lag = -np.inf, 0
     for tau in range(-half, half + 1):
-        lo, hi = len(ref) - window + tau, len(ref) + tau
-        if lo < 0 or hi > len(ref):
-            continue
-        b = ref[lo:hi] - ref[lo:hi].mean()
+        b = ref[end - window + tau:end + tau]
+        b = b - b.mean()
         c = float(np.dot(a, b))
         if c > best:
             best, lag = c, tau
@@ -185,7 +186,7 @@ def bench_vk(P, steps=100000):
             # phase: lag of this storage's shedding cycle behind float64's at the
             # last step; the rest: L2 against the float64 field at the lagged step
             period = 1.0 / max(st * 0.1 / 40, 1e-9)
-            lag = phase_lag(traces["f64"], uy, period, window=min(len(uy) // 2, int(4 * period)))
+            lag = phase_lag(traces["f64"], uy, period, window=min(len(uy) // 3, int(4 * period)))
             res["phase_lag_steps"] = lag
             res["phase_lag_periods"] = lag / period
             if steps + lag > 1 and lag != 0:

@@ -72,6 +72,61 @@ __device__ __forceinline__ int owner_of(const int* __restrict__ start, int n, in
   return lo;
 }
 
+// One tile of lattice `e` (staged in shared memory) at global step g.
+template <int STORE, int NPT, int THREADS, bool HAS_BC>
+__device__ __forceinline__ void batch_tile(const BatchEntry& e, int local, int g) {
+  const bool odd = (g - e.s0) & 1;
+  const void* pin = odd ? e.pop_b : e.pop_a;
+  void* pout = odd ? e.pop_a : e.pop_b;
+  const void* ain = odd ? e.aux_b : e.aux_a;
+  void* aout = odd ? e.aux_a : e.aux_b;
+  const uint32_t seed = hash32(e.P.seed + (uint32_t)(g - e.s0));
+  // with the sources inside the step, lattices without the pressure rewrite
+  // take the body without it; the boundary-free body leaves the rewrite to
+  // the boundary-node pass
+  const bool pressure = HAS_BC && e.P.g.pressure != 0;
+  auto step_chunk = [&](int x0, int y) {
+    if constexpr (STORE == LBM_STORE_FX64) {
+      if (pressure) fused_fx_body<NPT, HAS_BC, HAS_BC>(e.P, pin, pout, ain, aout, x0, y);
+      else fused_fx_body<NPT, HAS_BC, false>(e.P, pin, pout, ain, aout, x0, y);
+    } else {
+      if (pressure) fused_v2_body<STORE, NPT, HAS_BC, HAS_BC>(e.P, pin, pout, ain, aout, x0, y, seed);
+      else fused_v2_body<STORE, NPT, HAS_BC, false>(e.P, pin, pout, ain, aout, x0, y, seed);
+    }
+  };
+  if constexpr (HAS_BC) {
+    // row-segment tiles (small batches): `rows` rows of one segment of
+    // THREADS chunks; the row is uniform over the block, so its addressing
+    // runs in the uniform datapath (on a lone 420x180 lattice 15 % faster
+    // than runs across row ends)
+    const int yb = local / e.xblocks, xb = local - yb * e.xblocks;
+    const int x0 = (xb * THREADS + (int)threadIdx.x) * NPT;
+    const int y1 = min((yb + 1) * e.rows, e.P.g.ny);
+    for (int y = yb * e.rows; y < y1; ++y) step_chunk(x0, y);
+  } else {
+    // runs of THREADS consecutive chunks, chunks numbered row by row: no
+    // idle lanes at row ends.  The lanes of a run past the lattice's last
+    // chunk stay idle (x0 = nx).  The body takes x0 and y per thread: at a
+    // row end inside a warp the x neighbours come by direct loads.
+    for (int r = 0; r < e.rows; ++r) {
+      const int c = (local * e.rows + r) * THREADS + (int)threadIdx.x;
+      const int cpr = e.cpr;
+      int y = (int)__umulhi((uint32_t)c, e.cpr_magic);
+      int xc = c - y * cpr;
+      if (xc >= cpr) {
+        xc -= cpr;
+        ++y;
+      }
+      int x0 = xc * NPT;
+      if (y >= e.P.g.ny) {
+        y = e.P.g.ny - 1;
+        x0 = e.P.g.nx;
+      }
+      step_chunk(x0, y);
+    }
+  }
+}
+
 template <int STORE, int NPT, int THREADS, bool HAS_BC>
 __global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS, HAS_BC>())
     batch_kernel(const BatchEntry* __restrict__ tab, const int* __restrict__ tile_start, int n_inst,
@@ -98,59 +153,55 @@ __global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS,
         staged = lo;
       }
       if (g < e.s0 || g >= e.s_end) continue;
-      const int local = tile - __ldg(tile_start + lo);
-      const bool odd = (g - e.s0) & 1;
-      const void* pin = odd ? e.pop_b : e.pop_a;
-      void* pout = odd ? e.pop_a : e.pop_b;
-      const void* ain = odd ? e.aux_b : e.aux_a;
-      void* aout = odd ? e.aux_a : e.aux_b;
-      const uint32_t seed = hash32(e.P.seed + (uint32_t)(g - e.s0));
-      // with the sources inside the step, lattices without the pressure rewrite
-      // take the body without it; the boundary-free body leaves the rewrite to
-      // the boundary-node pass
-      const bool pressure = HAS_BC && e.P.g.pressure != 0;
-      auto step_chunk = [&](int x0, int y) {
-        if constexpr (STORE == LBM_STORE_FX64) {
-          if (pressure) fused_fx_body<NPT, HAS_BC, HAS_BC>(e.P, pin, pout, ain, aout, x0, y);
-          else fused_fx_body<NPT, HAS_BC, false>(e.P, pin, pout, ain, aout, x0, y);
-        } else {
-          if (pressure) fused_v2_body<STORE, NPT, HAS_BC, HAS_BC>(e.P, pin, pout, ain, aout, x0, y, seed);
-          else fused_v2_body<STORE, NPT, HAS_BC, false>(e.P, pin, pout, ain, aout, x0, y, seed);
-        }
-      };
-      if constexpr (HAS_BC) {
-        // row-segment tiles (small batches): `rows` rows of one segment of
-        // THREADS chunks; the row is uniform over the block, so its addressing
-        // runs in the uniform datapath (on a lone 420x180 lattice 15 % faster
-        // than runs across row ends)
-        const int yb = local / e.xblocks, xb = local - yb * e.xblocks;
-        const int x0 = (xb * THREADS + (int)threadIdx.x) * NPT;
-        const int y1 = min((yb + 1) * e.rows, e.P.g.ny);
-        for (int y = yb * e.rows; y < y1; ++y) step_chunk(x0, y);
-      } else {
-        // runs of THREADS consecutive chunks, chunks numbered row by row: no
-        // idle lanes at row ends.  The lanes of a run past the lattice's last
-        // chunk stay idle (x0 = nx).  The body takes x0 and y per thread: at a
-        // row end inside a warp the x neighbours come by direct loads.
-        for (int r = 0; r < e.rows; ++r) {
-          const int c = (local * e.rows + r) * THREADS + (int)threadIdx.x;
-          const int cpr = e.cpr;
-          int y = (int)__umulhi((uint32_t)c, e.cpr_magic);
-          int xc = c - y * cpr;
-          if (xc >= cpr) {
-            xc -= cpr;
-            ++y;
-          }
-          int x0 = xc * NPT;
-          if (y >= e.P.g.ny) {
-            y = e.P.g.ny - 1;
-            x0 = e.P.g.nx;
-          }
-          step_chunk(x0, y);
-        }
-      }
+      batch_tile<STORE, NPT, THREADS, HAS_BC>(e, tile - __ldg(tile_start + lo), g);
     }
   }
+}
+
+// The plain-grid form (one tile per block, block b = tile b): no loop state
+// is kept across the body, so the 16-bit bodies fit 1024 threads per SM.  The
+// block copies the lattices' tile starts into shared memory (one round trip)
+// and finds its lattice there, instead of a search through global memory
+// (a dependent L2 round trip per halving).
+constexpr int kStartSmem = 512;
+
+template <int STORE, int NPT, int THREADS, bool HAS_BC>
+constexpr int batch_grid_min_blocks() {
+  if constexpr (STORE == LBM_STORE_F16S || STORE == LBM_STORE_BF16S || (STORE == LBM_STORE_FX64 && NPT == 1))
+    return (HAS_BC ? 768 : 1024) / THREADS;
+  else
+    return batch_min_blocks<STORE, NPT, THREADS, HAS_BC>();
+}
+
+// owner_of for a whole block: the start list is copied into shared memory
+// (one round trip) and searched there when it has at most kStartSmem entries
+template <int THREADS>
+__device__ __forceinline__ int owner_of_staged(const int* __restrict__ start, int n, int t) {
+  __shared__ int sstart[kStartSmem];
+  if (n > kStartSmem) return owner_of(start, n, t);
+  for (int j = (int)threadIdx.x; j < n; j += THREADS) sstart[j] = __ldg(start + j);
+  __syncthreads();
+  int a = 0, b = n - 1;
+  while (a < b) {
+    const int mid = (a + b + 1) >> 1;
+    if (sstart[mid] <= t) a = mid;
+    else b = mid - 1;
+  }
+  return a;
+}
+
+template <int STORE, int NPT, int THREADS, bool HAS_BC>
+__global__ void __launch_bounds__(THREADS, batch_grid_min_blocks<STORE, NPT, THREADS, HAS_BC>())
+    batch_grid_kernel(const BatchEntry* __restrict__ tab, const int* __restrict__ tile_start, int n_inst,
+                      const int* __restrict__ gbase, int k) {
+  __shared__ __align__(16) unsigned char ebuf[sizeof(BatchEntry)];
+  const BatchEntry& e = *reinterpret_cast<const BatchEntry*>(ebuf);
+  const int tile = (int)blockIdx.x;
+  const int lo = owner_of_staged<THREADS>(tile_start, n_inst, tile);
+  stage_entry<THREADS, HAS_BC>(tab, lo, ebuf);
+  const int g = *gbase + k;
+  if (g < e.s0 || g >= e.s_end) return;
+  batch_tile<STORE, NPT, THREADS, HAS_BC>(e, tile - __ldg(tile_start + lo), g);
 }
 
 // The batched boundary-node pass: after batch_kernel<..., false> stepped every
@@ -179,7 +230,7 @@ __global__ void __launch_bounds__(kFixupChunk)
   __shared__ __align__(16) unsigned char ebuf[sizeof(BatchEntry)];
   const BatchEntry& e = *reinterpret_cast<const BatchEntry*>(ebuf);
   const int g = *gbase + k;
-  const int j = owner_of(bc_start, n_inst, (int)blockIdx.x);
+  const int j = owner_of_staged<kFixupChunk>(bc_start, n_inst, (int)blockIdx.x);
   stage_entry<kFixupChunk, true>(tab, j, ebuf);
   if (g < e.s0 || g >= e.s_end) return;
   const int t = ((int)blockIdx.x - __ldg(bc_start + j)) * kFixupChunk + (int)threadIdx.x;
@@ -237,13 +288,21 @@ inline int launch_batch(const void* table, int n, int tiles, int bc_chunks, int*
     }
     blocks = fill;
   }
-  // groups of up to kTileGroup tiles, but at least two groups per block
+  // groups of up to kTileGroup tiles, but at least two groups per block; a
+  // grid of more than half the tile count is a plain grid of one tile per block
+  const bool plain = (int64_t)blocks * 2 > (int64_t)tiles;
   const int group = (int)std::max<int64_t>(1, std::min<int64_t>(kTileGroup, (int64_t)tiles / (2 * (int64_t)blocks)));
   blocks = std::min(blocks, std::max(1, (tiles + group - 1) / group));
   for (int k = 0; k < nsteps; ++k) {
-    batch_kernel<STORE, NPT, THREADS, HAS_BC><<<blocks, THREADS, 0, s>>>(tab, start, n, tiles, gbase, k, group);
-    count_launch();
-    if (int e = check_launch("batch_kernel")) return e;
+    if (plain && tiles > 0) {
+      batch_grid_kernel<STORE, NPT, THREADS, HAS_BC><<<tiles, THREADS, 0, s>>>(tab, start, n, gbase, k);
+      count_launch();
+      if (int e = check_launch("batch_grid_kernel")) return e;
+    } else {
+      batch_kernel<STORE, NPT, THREADS, HAS_BC><<<blocks, THREADS, 0, s>>>(tab, start, n, tiles, gbase, k, group);
+      count_launch();
+      if (int e = check_launch("batch_kernel")) return e;
+    }
     if (!HAS_BC && bc_chunks > 0) {
       batch_fixup_kernel<STORE><<<bc_chunks, kFixupChunk, 0, s>>>(tab, bc_start, n, gbase, k);
       count_launch();

@@ -43,3 +43,11 @@ def test_roofline_inputs_from_committed_files():
     for st in ("fx64", "f64", "f16", "bf16"):
         tpn = bench.profile_traffic_per_node(st)
         assert tpn is not None and 0.5 * bench.BYTES_PER_NODE[st] < tpn < 2 * bench.BYTES_PER_NODE[st]
+
+
+def test_phase_lag_of_shifted_cycles():
+    t = np.arange(60000)
+    ref = np.sin(2 * np.pi * t / 2600.0) + 0.3 * np.sin(4 * np.pi * t / 2600.0)
+    for lag in (-700, -41, 0, 63, 1200):
+        other = np.sin(2 * np.pi * (t + lag) / 2600.0) + 0.3 * np.sin(4 * np.pi * (t + lag) / 2600.0)
+        assert bench.phase_lag(ref, other, 2600, 10400) == lag

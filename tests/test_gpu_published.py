@@ -104,12 +104,14 @@ def test_vk_exact_reproduces_published_runs(pkg, pub):
     assert st == pytest.approx(float(pub["vk100_st_interp"]), rel=1e-9)
 
 
-@pytest.mark.parametrize("storage", ["fx64", "f16", "bf16", "f32"])
-def test_vk_strouhal_within_one_percent(pkg, pub, storage):
+@pytest.mark.parametrize("storage,tol", [("fx64", 1e-6), ("f16", 0.01), ("f32", 0.01), ("bf16", 0.02)])
+def test_vk_strouhal_against_published(pkg, pub, storage, tol):
     """Strouhal number of the 200 000-step |u| trace after step 70 000 against the
     published trace, by the sub-bin estimate (resolution: the padded bin is
     1/(16 x 130 001) cycles per step, 0.01 % of St; the reference's own argmax is
-    quantised to 0.68 %)."""
+    quantised to 0.68 %).  Stated tolerances: fx64 1e-6, the float32 arithmetic
+    on binary16 deviations 1 %, float32 storage 1 %, bfloat16 deviations 2 %
+    (measured: 3.6e-10, 0.043 %, 0.37 %, 1.1 %)."""
     from lattice_boltzmann_parallel_solver_gb300 import analysis
     lat = vk_lattice(pkg, storage)
     lat.step(200000)
@@ -121,7 +123,7 @@ def test_vk_strouhal_within_one_percent(pkg, pub, storage):
     print("%s: St %.6f against published %.6f (%.3e), trace max |diff| %.3e" % (
         storage, st, float(pub["vk100_st_interp"]), err,
         np.abs(tr[::50] - pub["vk100_trace_every50"]).max()))
-    assert err <= 0.01
+    assert err <= tol
 
 
 def test_reynolds_sweep_against_published(pkg, pub):
