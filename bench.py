@@ -44,7 +44,8 @@ def parse():
                    help="boundary sources: a separate pass over the boundary nodes (split), inside the step "
                         "(inline), or chosen by the lattice size (auto)")
     p.add_argument("--no-extras", action="store_true", help="skip variants, e2e, CPU baseline and the other configs")
-    p.add_argument("--workload", default="cavity", choices=["cavity", "shear", "vk", "batch", "serve", "batch_step"],
+    p.add_argument("--workload", default="cavity",
+                   choices=["cavity", "shear", "vk", "batch", "serve", "serve_sweep", "batch_step"],
                    help="cavity: the headline line; the others print one config's results and exit")
     p.add_argument("--configs", default="shear,vk,batch,serve", help="other configs added to the headline line")
     return p.parse_args()
@@ -134,7 +135,8 @@ def phase_lag(ref, other, period_guess, window):
     for tau in range(-half, half + 1):
         b = ref[end - window + tau:end + tau]
         b = b - b.mean()
-        c = float(np.dot(a, b))
+        # normalised: a window of larger amplitude must not win by its energy
+        c = float(np.dot(a, b)) / max(float(np.linalg.norm(b)), 1e-300)
         if c > best:
             best, lag = c, tau
     return lag
@@ -251,9 +253,9 @@ def bench_batch(P, steps=20000, n=256):
 
 
 def batch_step(P, steps=8):
-    """The 256-lattice batch (f16, 4 nodes per thread, 64 threads, 2 rows per
-    tile) set up and advanced a few steps without the autotuner: the case the
-    batch kernel's ncu capture runs."""
+    """The 256-lattice batch (f16, 4 nodes per thread, 128 threads, 8 runs per
+    tile, one tile per block: the autotuner's pick) set up and advanced a few
+    steps without the autotuner: the case the batch kernels' ncu captures run."""
     import torch
     from lattice_boltzmann_parallel_solver_gb300.batch import Batch, Member
     params = P.scenarios.batch_sweep_params(256)
@@ -261,43 +263,77 @@ def batch_step(P, steps=8):
     for j, q in enumerate(params):
         f, rho, u, om, bnd = P.scenarios.von_karman_device(q["nx"], q["ny"], q["plate"], q["re"], seed=j)
         members.append(Member(q["nx"], q["ny"], om, bnd, steps=2 * steps, f0=f, rho0=rho, u0=u))
-    b = Batch(members, storage="f16", npt=4, threads=64, rows=2).start()
+    from lattice_boltzmann_parallel_solver_gb300.batch import ONE_TILE_PER_BLOCK
+    b = Batch(members, storage="f16", npt=4, threads=128, rows=8, blocks=ONE_TILE_PER_BLOCK).start()
     ms = timed_ms(lambda: b.run(steps))
     torch.cuda.synchronize()
-    return {"workload": "256 von Karman lattices, f16, npt 4, 64 threads, 2 rows, %d steps (no autotuning)" % steps,
-            "nodes": b.nodes, "ms_per_step": ms / steps}
+    return {"workload": "256 von Karman lattices, f16, npt 4, 128 threads, 8 runs per tile, one tile per block, "
+                        "%d steps (no autotuning)" % steps, "nodes": b.nodes, "ms_per_step": ms / steps}
 
 
-def bench_serve(P, n16=200, n64=40):
-    """Serving: seeded Poisson arrivals at 50/s of Couette / Poiseuille / von
-    Karman requests with 1k-50k steps, continuous batching under an HBM budget;
-    f16 storage against plain float64 (f64 storage) and fx64; error of f16
-    results against their solo fx64 solve on a sample."""
+def serve_rate(P, storage, rate, n, seed=7):
+    """One run of the serving loop: the first n requests of the seeded stream
+    (the same requests for every storage and rate), arriving as a Poisson stream
+    of the given mean rate."""
     import torch
     from lattice_boltzmann_parallel_solver_gb300.serving import ServingEngine, request_mix, summarize
+    reqs = request_mix(n, rate=rate, seed=seed, lazy=True)
+    eng = ServingEngine(storage=storage, hbm_budget=64 << 30, tick_steps=500)
+    done = eng.serve(reqs, realtime=True)
+    s = summarize(done)
+    s.update({"offered_per_s": rate, "arrival_window_s": reqs[-1].arrival, "max_live": eng.stats["max_live"]})
+    # latency of the second half of the stream: past the start-up transient
+    lat = sorted(r.latency for r in done if r.rid >= n // 2)
+    s["p99_second_half_s"] = float(np.percentile(lat, 99))
+    return s, done
+
+
+def bench_serve(P, n=60, rates=None):
+    """Serving: seeded Poisson arrivals of Couette / Poiseuille / von Karman
+    requests with 1k-50k steps, continuous batching under an HBM budget; the
+    same n requests through f16 storage, fx64 and plain float64 (f64), each at
+    offered loads below its capacity (per-rate rows); error of f16 results
+    against their solo fx64 solve on a sample."""
+    import torch
+    rates = rates or {"f16": (8.0, 14.0), "fx64": (3.0,), "f64": (1.0,)}
     out = {}
-    for storage, n in (("f16", n16), ("fx64", n64), ("f64", n64)):
-        reqs = request_mix(n, rate=50.0, seed=7)
-        eng = ServingEngine(storage=storage, hbm_budget=64 << 30, tick_steps=500)
-        done = eng.serve(reqs, realtime=True)
-        s = summarize(done)
-        s["max_live"] = eng.stats["max_live"]
-        out[storage] = s
-        if storage == "f16":
-            errs, budget = {}, 0.0
-            for r in sorted(done, key=lambda r: r.nodes * r.steps):
-                if budget > 20.0 or len(errs) >= 9:
-                    break
-                lat = P.Lattice(r.nx, r.ny, r.omega, r.boundary, storage="fx64").set_state(r.f0, r.rho0, r.u0)
-                t = timed_ms(lambda: lat.step(r.steps)) / 1e3
-                budget += t
-                u64 = lat.moments()[1]
-                errs.setdefault(r.kind, []).append(float(torch.linalg.norm(r.u - u64) / torch.linalg.norm(u64)))
-            out["f16_velocity_l2_rel_err_vs_solo_fx64"] = {k: max(v) for k, v in errs.items()}
-        del done, reqs
-        torch.cuda.empty_cache()
-    return {"workload": "Poisson 50 req/s mix of Couette / Poiseuille / von Karman, 1k-50k steps, "
-                        "HBM budget 64 GB", "results": out}
+    for storage, rs in rates.items():
+        rows = []
+        for rate in rs:
+            s, done = serve_rate(P, storage, rate, n)
+            rows.append(s)
+            if storage == "f16" and rate == rs[0]:
+                errs, budget = {}, 0.0
+                for r in sorted(done, key=lambda r: r.nodes * r.steps):
+                    if budget > 20.0 or len(errs) >= 9:
+                        break
+                    lat = P.Lattice(r.nx, r.ny, r.omega, r.boundary, storage="fx64").set_state(*r.initial_state())
+                    t = timed_ms(lambda: lat.step(r.steps)) / 1e3
+                    budget += t
+                    u64 = lat.moments()[1]
+                    errs.setdefault(r.kind, []).append(float(torch.linalg.norm(r.u - u64) / torch.linalg.norm(u64)))
+                    del lat
+                out["f16_velocity_l2_rel_err_vs_solo_fx64"] = {k: max(v) for k, v in errs.items()}
+            del done
+            torch.cuda.empty_cache()
+        out[storage] = rows
+    return {"workload": "the same %d seeded requests (Couette / Poiseuille / von Karman, 1k-50k steps) at "
+                        "each offered Poisson rate, HBM budget 64 GB" % n, "results": out}
+
+
+def bench_serve_sweep(P, window_s=60.0):
+    """Offered load swept up to and beyond each storage's capacity, every rate
+    with at least ``window_s`` seconds of arrivals (n = rate x window requests,
+    a prefix of one seeded stream): solves/s, p50 and p99 latency per rate."""
+    rates = {"f16": (4.0, 8.0, 12.0, 16.0, 20.0), "fx64": (1.5, 3.0, 4.5, 6.0), "f64": (0.5, 1.0, 1.5, 2.0)}
+    out = {}
+    for storage, rs in rates.items():
+        out[storage] = []
+        for rate in rs:
+            s, done = serve_rate(P, storage, rate, max(60, int(rate * window_s)))
+            out[storage].append(s)
+            del done
+    return {"workload": "offered-load sweep, >= %.0f s of arrivals per rate" % window_s, "results": out}
 
 
 def peaks():
@@ -479,7 +515,7 @@ def main():
     torch.cuda.set_device(local)
     if args.workload != "cavity":
         fn = {"shear": bench_shear, "vk": bench_vk, "batch": bench_batch, "serve": bench_serve,
-              "batch_step": batch_step}[args.workload]
+              "serve_sweep": bench_serve_sweep, "batch_step": batch_step}[args.workload]
         print(json.dumps(fn(P)), flush=True)
         return
     if world > 1:

@@ -74,6 +74,17 @@ typedef struct lbm_geometry {
    * LBM_FLAG_BC_INLINE applies the sources inside the step. */
   const int32_t* bcnodes;
   int32_t n_bcnodes;
+  /* Plain inlet and outlet columns (all zero: none).  edge_inlet_desc is the
+   * descriptor of the nodes of column 0 that take only the inlet populations
+   * (all nine directions CONST from one constant set), edge_outlet_desc that
+   * of the nodes of column nx-1 that take only directions 3, 6, 7 from the
+   * outlet memory (the others stream); each is set only when every node of
+   * its column has a descriptor.  The last n_bcnodes_edge entries of bcnodes
+   * are the nodes with these two descriptors (the others come first).  The
+   * batched step applies them inside its boundary-free launch, where they cost
+   * no scattered column accesses, and passes over the other entries only. */
+  uint32_t edge_inlet_desc, edge_outlet_desc;
+  int32_t n_bcnodes_edge;
 } lbm_geometry;
 
 /* ---- storage / arithmetic of the resident state ------------------------- */

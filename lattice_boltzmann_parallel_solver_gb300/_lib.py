@@ -47,6 +47,7 @@ class Geometry(C.Structure):
         ("rho_in", f64), ("rho_out", f64),
         ("outlet", i32),
         ("bcnodes", vp), ("n_bcnodes", i32),
+        ("edge_inlet_desc", C.c_uint32), ("edge_outlet_desc", C.c_uint32), ("n_bcnodes_edge", i32),
     ]
 
 

@@ -85,13 +85,15 @@ __device__ __forceinline__ void batch_tile(const BatchEntry& e, int local, int g
   // take the body without it; the boundary-free body leaves the rewrite to
   // the boundary-node pass
   const bool pressure = HAS_BC && e.P.g.pressure != 0;
+  // the boundary-free body applies the plain inlet / outlet columns itself
+  // (EDGES), the boundary-node pass the other boundary nodes
   auto step_chunk = [&](int x0, int y) {
     if constexpr (STORE == LBM_STORE_FX64) {
-      if (pressure) fused_fx_body<NPT, HAS_BC, HAS_BC>(e.P, pin, pout, ain, aout, x0, y);
-      else fused_fx_body<NPT, HAS_BC, false>(e.P, pin, pout, ain, aout, x0, y);
+      if (pressure) fused_fx_body<NPT, HAS_BC, HAS_BC, !HAS_BC>(e.P, pin, pout, ain, aout, x0, y);
+      else fused_fx_body<NPT, HAS_BC, false, !HAS_BC>(e.P, pin, pout, ain, aout, x0, y);
     } else {
-      if (pressure) fused_v2_body<STORE, NPT, HAS_BC, HAS_BC>(e.P, pin, pout, ain, aout, x0, y, seed);
-      else fused_v2_body<STORE, NPT, HAS_BC, false>(e.P, pin, pout, ain, aout, x0, y, seed);
+      if (pressure) fused_v2_body<STORE, NPT, HAS_BC, HAS_BC, !HAS_BC>(e.P, pin, pout, ain, aout, x0, y, seed);
+      else fused_v2_body<STORE, NPT, HAS_BC, false, !HAS_BC>(e.P, pin, pout, ain, aout, x0, y, seed);
     }
   };
   if constexpr (HAS_BC) {
@@ -205,13 +207,14 @@ __global__ void __launch_bounds__(THREADS, batch_grid_min_blocks<STORE, NPT, THR
 }
 
 // The batched boundary-node pass: after batch_kernel<..., false> stepped every
-// node of every live lattice without boundary sources or pressure rewrite, one
-// thread per pass node recomputes that node with them and overwrites its
-// outputs (the body at one node per thread, the same arithmetic and random
-// bits as the in-step sources).  A lattice's pass nodes are its listed boundary
-// nodes, then, under the pressure rewrite, columns 1 and nx-2 of every row
-// (those not listed already), whose nodes write the rewritten populations of
-// columns nx-1 and 0.  Block b takes chunk b of the chunk list: lattice j owns
+// node of every live lattice without boundary sources or pressure rewrite
+// (but with the plain inlet / outlet columns), one thread per pass node
+// recomputes that node with them and overwrites its outputs (the body at one
+// node per thread, the same arithmetic and random bits as the in-step
+// sources).  A lattice's pass nodes are its listed boundary nodes other than
+// the plain edge nodes, then, under the pressure rewrite, columns 1 and nx-2 of
+// every row (those not listed already), whose nodes write the rewritten
+// populations of columns nx-1 and 0.  Block b takes chunk b of the chunk list: lattice j owns
 // chunks [bc_start[j], bc_start[j + 1]) of kFixupChunk pass nodes.
 constexpr int kFixupChunk = 128;
 
@@ -220,7 +223,7 @@ constexpr int kFixupChunk = 128;
 constexpr int64_t kBatchSplitNodes = (int64_t)1 << 20;
 
 inline int64_t pass_nodes(const GeoK& g) {
-  return (g.bcmask != nullptr ? (int64_t)g.n_bcnodes : 0) + (g.pressure ? 2 * (int64_t)g.ny : 0);
+  return (g.bcmask != nullptr ? (int64_t)(g.n_bcnodes - g.n_bcnodes_edge) : 0) + (g.pressure ? 2 * (int64_t)g.ny : 0);
 }
 
 template <int STORE>
@@ -235,7 +238,7 @@ __global__ void __launch_bounds__(kFixupChunk)
   if (g < e.s0 || g >= e.s_end) return;
   const int t = ((int)blockIdx.x - __ldg(bc_start + j)) * kFixupChunk + (int)threadIdx.x;
   const int nx = e.P.g.nx;
-  const int listed = e.P.g.bcmask != nullptr ? e.P.g.n_bcnodes : 0;
+  const int listed = e.P.g.bcmask != nullptr ? e.P.g.n_bcnodes - e.P.g.n_bcnodes_edge : 0;
   int x, y;
   if (t < listed) {
     const int node = __ldg(e.P.g.bcnodes + t);
@@ -248,7 +251,8 @@ __global__ void __launch_bounds__(kFixupChunk)
     y = q >> 1;
     x = (q & 1) ? nx - 2 : 1;
     if ((q & 1) && nx - 2 == 1) return;  // one column: its even entry covers it
-    if (e.P.g.bcmask != nullptr && ((__ldg(e.P.g.bcmask + y * e.P.g.words + (x >> 5)) >> (x & 31)) & 1u))
+    if (e.P.g.bcmask != nullptr && ((__ldg(e.P.g.bcmask + y * e.P.g.words + (x >> 5)) >> (x & 31)) & 1u) &&
+        !plain_edge_node(e.P, x, y))
       return;  // listed already
   }
   const bool odd = (g - e.s0) & 1;

@@ -25,6 +25,10 @@ struct GeoK {
   double cconst[LBM_MAX_SETS][9];
   const int32_t* bcnodes;
   int n_bcnodes;
+  // plain inlet / outlet columns (lbm_geometry), and the inlet's populations
+  uint32_t edge_in_desc, edge_out_desc;
+  int n_bcnodes_edge;
+  double edge_in_f[9];
 };
 
 struct View {
@@ -70,14 +74,23 @@ __device__ __forceinline__ uint32_t launch_seed(const KParams& P) {
   return P.step_dev != nullptr ? hash32(P.seed + (uint32_t)__ldg(P.step_dev)) : P.seed;
 }
 
+// a node the body applies as a plain inlet / outlet node itself (edges on)
+__device__ __forceinline__ bool plain_edge_node(const KParams& P, int x, int y) {
+  const uint32_t want = x == 0 ? P.g.edge_in_desc : (x == P.g.nx - 1 ? P.g.edge_out_desc : 0u);
+  return want != 0u && __ldg(P.g.desc + y * P.g.nx + x) == want;
+}
+
 // skip_bc: a body without its boundary block leaves the probe of a node that
-// the batched boundary-node pass recomputes (a listed boundary node or, under
-// the pressure rewrite, a node of column 1 or nx-2) to that pass
+// the batched boundary-node pass recomputes (a listed boundary node other than
+// the plain edge nodes the body applies itself when ``edges`` is set, or,
+// under the pressure rewrite, a node of column 1 or nx-2) to that pass
 template <typename R>
-__device__ __forceinline__ void write_probe(const KParams& P, int x, int y, R ux, R uy, bool skip_bc = false) {
+__device__ __forceinline__ void write_probe(const KParams& P, int x, int y, R ux, R uy, bool skip_bc = false,
+                                            bool edges = false) {
   if (P.probe_buf != nullptr && x == P.probe_x && y == P.probe_y) {
     if (skip_bc && ((P.g.pressure && (x == 1 || x == P.g.nx - 2)) ||
-                    (P.g.bcmask != nullptr && ((__ldg(P.g.bcmask + y * P.g.words + (x >> 5)) >> (x & 31)) & 1u))))
+                    (P.g.bcmask != nullptr && ((__ldg(P.g.bcmask + y * P.g.words + (x >> 5)) >> (x & 31)) & 1u) &&
+                     !(edges && plain_edge_node(P, x, y)))))
       return;
     const int t = *P.probe_count;
     if (t < P.probe_cap) {
@@ -100,7 +113,7 @@ __device__ __forceinline__ void write_probe(const KParams& P, int x, int y, R ux
 // 32-bit element indices (9 * plane < 2^31).  Boundary descriptors and the
 // pressure rewrite are compiled in only where a geometry may have them.
 // ---------------------------------------------------------------------------
-template <int STORE, int NPT, bool HAS_BC, bool HAS_PRESSURE>
+template <int STORE, int NPT, bool HAS_BC, bool HAS_PRESSURE, bool EDGES = false>
 __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_in_v, void* pop_out_v,
                                               const void* aux_in_v, void* aux_out_v, int x0, int y,
                                               uint32_t seed) {
@@ -183,6 +196,27 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     }
   }
 
+  if constexpr (EDGES && !HAS_BC) {
+    // the plain inlet / outlet columns, applied to every node of column 0 /
+    // nx-1 (the pass recomputes the ones with other sources)
+    if (first && P.g.edge_in_desc != 0u) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) f[i][0] = work_of_f((R)P.g.edge_in_f[i], i);
+    }
+    if (last && P.g.edge_out_desc != 0u && aux_in_v != nullptr) {
+      const R* aux_in = static_cast<const R*>(aux_in_v);
+      const int kl = nx - 1 - x0;
+      const R a3 = work_of_f(aux_in[0 * ny + y], 3), a6 = work_of_f(aux_in[1 * ny + y], 6),
+              a7 = work_of_f(aux_in[2 * ny + y], 7);
+#pragma unroll
+      for (int k = 0; k < NPT; ++k) {
+        f[3][k] = k == kl ? a3 : f[3][k];
+        f[6][k] = k == kl ? a6 : f[6][k];
+        f[7][k] = k == kl ? a7 : f[7][k];
+      }
+    }
+  }
+
   if (has_bc) {
     const uint32_t bits = (bcword >> (x0 & 31)) & ((NPT >= 32) ? 0xffffffffu : ((1u << NPT) - 1u));
     if (bits) {
@@ -238,7 +272,7 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
         up[0] = (double)ux;
         up[P.u_out.sc] = (double)uy;
       }
-      write_probe(P, x, y, ux, uy, !HAS_BC);
+      write_probe(P, x, y, ux, uy, !HAS_BC, EDGES);
     }
     if (HAS_PRESSURE && P.g.pressure && k < nvalid && (x == nx - 2 || x == 1)) {
       R br[9];
@@ -360,7 +394,7 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
 // the pressure rewrite of columns 0 / nx-1 use float64 on the converted values.
 // The outlet memory holds the stored integers, as in the generic kernel.
 // ---------------------------------------------------------------------------
-template <int NPT, bool HAS_BC, bool HAS_PRESSURE>
+template <int NPT, bool HAS_BC, bool HAS_PRESSURE, bool EDGES = false>
 __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_in_v, void* pop_out_v,
                                               const void* aux_in_v, void* aux_out_v, int x0, int y) {
   using T = long long;
@@ -417,6 +451,26 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
             f[i][k] = __ldg(base + xs);
           }
         }
+      }
+    }
+  }
+
+  if constexpr (EDGES && !HAS_BC) {
+    // the plain inlet / outlet columns, applied to every node of column 0 /
+    // nx-1 (the pass recomputes the ones with other sources)
+    if (first && P.g.edge_in_desc != 0u) {
+#pragma unroll
+      for (int i = 0; i < 9; ++i) f[i][0] = fx::to_fx(P.g.edge_in_f[i], wd(i));
+    }
+    if (last && P.g.edge_out_desc != 0u && aux_in_v != nullptr) {
+      const T* aux_in = static_cast<const T*>(aux_in_v);
+      const int kl = nx - 1 - x0;
+      const T a3 = aux_in[0 * ny + y], a6 = aux_in[1 * ny + y], a7 = aux_in[2 * ny + y];
+#pragma unroll
+      for (int k = 0; k < NPT; ++k) {
+        f[3][k] = k == kl ? a3 : f[3][k];
+        f[6][k] = k == kl ? a6 : f[6][k];
+        f[7][k] = k == kl ? a7 : f[7][k];
       }
     }
   }
@@ -486,7 +540,7 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
           up[0] = ux;
           up[P.u_out.sc] = uy;
         }
-        write_probe(P, x, y, ux, uy, !HAS_BC);
+        write_probe(P, x, y, ux, uy, !HAS_BC, EDGES);
       }
     }
     if (!fx::collide_q(g, P.qc)) {
@@ -590,6 +644,20 @@ inline bool to_geok(const lbm_geometry* g, GeoK& k) {
   std::memcpy(k.cconst, g->cconst, sizeof(k.cconst));
   k.bcnodes = g->n_bcnodes > 0 ? g->bcnodes : nullptr;
   k.n_bcnodes = k.bcnodes != nullptr ? g->n_bcnodes : 0;
+  if (g->n_bcnodes_edge < 0 || g->n_bcnodes_edge > k.n_bcnodes)
+    return set_error(LBM_ERR_ARG, "n_bcnodes_edge out of range"), false;
+  if (g->edge_inlet_desc != 0u && (g->edge_inlet_desc & 0x3FFFFu) != 0x2AAAAu)
+    return set_error(LBM_ERR_ARG, "edge_inlet_desc is not an all-CONST descriptor"), false;
+  if (g->edge_outlet_desc != 0u && (g->edge_outlet_desc & 0x3FFFFu) != 0xF0C0u)
+    return set_error(LBM_ERR_ARG, "edge_outlet_desc is not the plain outlet descriptor"), false;
+  if (k.bcmask != nullptr) {
+    k.edge_in_desc = g->edge_inlet_desc;
+    k.edge_out_desc = g->nx >= 2 ? g->edge_outlet_desc : 0u;
+    k.n_bcnodes_edge = g->n_bcnodes_edge;
+    const int cs = (int)((g->edge_inlet_desc >> LBM_DESC_CSET_SHIFT) & 15u);
+    if (k.edge_in_desc != 0u)
+      for (int i = 0; i < 9; ++i) k.edge_in_f[i] = g->cconst[cs][i];
+  }
   return true;
 }
 

@@ -79,11 +79,19 @@ class CompiledGeometry:
             self.bcmask = torch.from_numpy(np.ascontiguousarray(bcmask)).to(device)
             g.desc = self.desc.data_ptr()
             g.bcmask = self.bcmask.data_ptr()
-            # linear indices y*nx + x of the boundary nodes, for the boundary-node pass
-            nodes = np.flatnonzero(special.T.reshape(-1)).astype(np.int32)
+            # plain inlet / outlet columns: the batched boundary-free step applies
+            # them itself, its boundary-node pass skips them
+            edge = np.zeros((nx, ny), dtype=bool)
+            g.edge_inlet_desc, g.edge_outlet_desc = self._edge_desc(src, desc, special, edge)
+            # linear indices y*nx + x of the boundary nodes, for the boundary-node
+            # pass: the other boundary nodes first, then the plain edge nodes
+            core = np.flatnonzero((special & ~edge).T.reshape(-1))
+            tail = np.flatnonzero(edge.T.reshape(-1))
+            nodes = np.concatenate([core, tail]).astype(np.int32)
             self.bcnodes = torch.from_numpy(nodes).to(device)
             g.bcnodes = self.bcnodes.data_ptr()
             g.n_bcnodes = int(nodes.size)
+            g.n_bcnodes_edge = int(tail.size)
             g.n_kset, g.n_cset = len(ktab), len(ctab)
             for s in range(len(ktab)):
                 for i in range(9):
@@ -102,6 +110,31 @@ class CompiledGeometry:
             assert nx >= 2
         self.pressure = pressure
         self.struct = g
+
+    @staticmethod
+    def _edge_desc(src, desc, special, edge):
+        """(inlet, outlet) descriptors of the plain edge nodes, 0 for none; marks
+        those nodes in ``edge``.  Plain inlet: all nine sources CONST (the most
+        common such descriptor of column 0); plain outlet: directions 3, 6, 7
+        OUTLET and the others PULL (column nx-1).  A column qualifies only when
+        every node of it has a descriptor, so that a kernel may apply the form
+        to the whole column and leave the other nodes to the pass."""
+        nx = src.shape[0]
+        out = []
+        for x, want in ((0, np.full(9, CONST)),
+                        (nx - 1, np.array([OUTLET if i in (3, 6, 7) else PULL for i in range(9)]))):
+            if nx < 2 or not special[x, :].all():
+                out.append(0)
+                continue
+            plain = (src[x] == want.astype(np.uint32)).all(axis=-1)
+            if not plain.any():
+                out.append(0)
+                continue
+            vals, counts = np.unique(desc[x, plain], return_counts=True)
+            d = int(vals[np.argmax(counts)])
+            edge[x, :] |= plain & (desc[x, :] == d)
+            out.append(d)
+        return out[0], out[1]
 
     @property
     def ref(self):

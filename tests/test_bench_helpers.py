@@ -51,3 +51,10 @@ def test_phase_lag_of_shifted_cycles():
     for lag in (-700, -41, 0, 63, 1200):
         other = np.sin(2 * np.pi * (t + lag) / 2600.0) + 0.3 * np.sin(4 * np.pi * (t + lag) / 2600.0)
         assert bench.phase_lag(ref, other, 2600, 10400) == lag
+
+
+def test_phase_lag_is_not_pulled_by_a_growing_amplitude():
+    t = np.arange(100000)
+    ref = (1 + t / 2e4) * np.sin(2 * np.pi * t / 2600.0)
+    assert bench.phase_lag(ref, ref.copy(), 2600, 10400) == 0
+    assert bench.phase_lag(ref, (1 + (t + 25) / 2e4) * np.sin(2 * np.pi * (t + 25) / 2600.0), 2600, 10400) == 25

@@ -146,28 +146,63 @@ def test_too_many_constant_sets():
         CompiledGeometry(lx, ly, src, device="cpu")
 
 
-@pytest.mark.parametrize("name", ["couette", "poiseuille", "cavity", "vk"])
+@pytest.mark.parametrize("name", ["couette", "poiseuille", "cavity", "vk", "channel"])
 def test_boundary_node_list_matches_the_mask(name):
     """The boundary-node pass recomputes exactly the listed nodes: the list
-    holds the linear indices y*nx + x of the mask's set bits, ascending, and
+    holds the linear indices y*nx + x of the mask's set bits, the plain inlet
+    and outlet nodes (n_bcnodes_edge of them) last, each part ascending, and
     covers at most an eighth of these lattices."""
     lx, ly = 70, 33
+    feq_in = O.inlet_populations((1, 1), 1.0, 0.1)[0, 0]
     if name == "couette":
         b = BU.couette_flow_boundary_conditions(lx, ly, 0.05, 1.0)
     elif name == "poiseuille":
         b = BU.poiseuille_flow_boundary_conditions(lx, ly, 0.34, 0.33)
     elif name == "cavity":
         b = BU.cavity_boundary_conditions(lx, ly, 0.1, 1.0)
-    else:
-        feq_in = O.inlet_populations((1, 1), 1.0, 0.1)[0, 0]
+    elif name == "vk":
         b = BU.Boundary(BU._vk_closures(lx, ly, 1.0, 0.1, 8, feq_in=feq_in))
+    else:
+        b = BU.Boundary(BU._vk_closures(lx, ly, 1.0, 0.1, 8, feq_in=feq_in, walls=True, plate_offset=1))
     g = compiled(b, lx, ly)
     mask = g.bcmask.cpu().numpy()
     bits = ((mask[:, :, None] >> np.arange(32, dtype=np.uint32)) & 1).reshape(ly, -1)[:, :lx].astype(bool)
     want = np.flatnonzero(bits.reshape(-1))
     got = g.bcnodes.cpu().numpy()
-    assert got.dtype == np.int32 and np.array_equal(got, want)
+    n_edge = g.struct.n_bcnodes_edge
+    core, tail = got[:got.size - n_edge], got[got.size - n_edge:]
+    assert got.dtype == np.int32 and np.array_equal(np.sort(got), want)
+    assert np.all(np.diff(core) > 0) and np.all(np.diff(tail) > 0)
     assert g.struct.n_bcnodes == want.size and 0 < want.size * 8 <= lx * ly
+    desc = g.desc.cpu().numpy().reshape(-1)
+    if name in ("vk", "channel"):
+        # every inlet / outlet node without other sources is a plain edge node
+        edge_rows = ly if name == "vk" else ly - 2
+        assert n_edge == 2 * edge_rows
+        x = tail % lx
+        assert set(x.tolist()) == {0, lx - 1}
+        assert np.all(desc[tail[x == 0]] == g.struct.edge_inlet_desc)
+        assert np.all(desc[tail[x == lx - 1]] == g.struct.edge_outlet_desc)
+        assert g.struct.edge_inlet_desc & 0x3FFFF == 0x2AAAA and g.struct.edge_outlet_desc & 0x3FFFF == 0xF0C0
+        # the corners (walls over inlet / outlet) stay in the pass
+        assert not np.isin(tail, core).any()
+    else:
+        assert n_edge == 0 and g.struct.edge_inlet_desc == 0 and g.struct.edge_outlet_desc == 0
+
+
+def test_edge_columns_need_a_descriptor_on_every_node():
+    """An inlet on part of column 0 is no plain edge column: the kernel would
+    apply it to the nodes without one."""
+    lx, ly = 20, 10
+    m = np.zeros((lx, ly), dtype=bool)
+    m[0, 2:8] = True
+    src = [(m, i, CONST, 0.1 + 0.01 * i) for i in range(9)]
+    g = CompiledGeometry(lx, ly, src, device="cpu")
+    assert g.struct.edge_inlet_desc == 0 and g.struct.n_bcnodes_edge == 0
+    m[0, :] = True
+    src = [(m, i, CONST, 0.1 + 0.01 * i) for i in range(9)]
+    g = CompiledGeometry(lx, ly, src, device="cpu")
+    assert g.struct.edge_inlet_desc != 0 and g.struct.n_bcnodes_edge == ly
 
 
 @pytest.mark.parametrize("offset", [0, 1])

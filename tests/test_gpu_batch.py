@@ -134,6 +134,32 @@ def test_boundary_node_pass_equals_inline_sources(pkg, storage):
             assert ta.shape[0] == m.steps - 1 and torch.equal(ta, tb), (storage, j)
 
 
+@pytest.mark.parametrize("storage", ["fx64", "f16", "f32"])
+@pytest.mark.parametrize("probe", [(202, 30), (0, 0), (202, 61), (0, 17), (1, 17), (201, 30)])
+def test_plain_edge_columns_equal_inline_sources(pkg, storage, probe):
+    """The batched boundary-free step applies the plain inlet and outlet columns
+    itself and the pass skips them: bit-identical to the sources inside the
+    step, with the probe on a plain outlet node, on the corners where the walls
+    override the inlet / outlet (nodes the pass recomputes), on a plain inlet
+    node and next to both columns."""
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch
+    npt = {"fx64": 1, "f32": 2}.get(storage, 4)
+    runs = []
+    for inline in (True, False):
+        ms = members(pkg, steps=(60, 3, 3, 3, 3))[:1]
+        ms[0].probe = probe
+        b = Batch(ms, storage=storage, npt=npt, threads=64, rows=2, inline_bc=inline).start()
+        if not inline:
+            g = ms[0].geo.struct
+            assert g.n_bcnodes_edge == 2 * (62 - 2) and g.edge_inlet_desc and g.edge_outlet_desc
+        b.run()
+        runs.append(b)
+    a, b = runs
+    assert torch.equal(a.read(0)[0], b.read(0)[0])
+    ta, tb = a.probe_trace(0), b.probe_trace(0)
+    assert ta.shape[0] == 59 and torch.equal(ta, tb)
+
+
 def test_batch_plan_follows_the_size(pkg):
     """Below 2^20 nodes in total a batch keeps the boundary sources inside one
     launch per step; from 2^20 it runs the boundary-free step and the pass."""
