@@ -247,6 +247,8 @@ def bench_batch(P, steps=20000, n=256):
     best = min(tune, key=lambda r: r["ms_per_step"])
     return {"workload": "%d von Karman lattices, %d steps each, %.1f M nodes, f16 storage" % (n, steps, nodes / 1e6),
             "aggregate_mlups": agg, "batch_wall_s": ms / 1e3, "autotuned": best,
+            "hbm_frac": agg * 1e6 * 36 / 1e9 / peaks()[0],
+            "fastest_candidates": sorted(tune, key=lambda r: r["ms_per_step"])[:8],
             "candidates": len(tune), "sequential": seq,
             "omega_range": [min(q["omega"] for q in params), max(q["omega"] for q in params)],
             "stability_risk_instances": sum(q["risky"] for q in params)}

@@ -163,9 +163,10 @@ int lbm_step_f64_host(const lbm_geometry* g, const double* f, const double* rho,
  * library, which every GPU that loads the library holds until the process
  * exits.  A lattice needing more scratch than that, (9*pitch*ny + 3*ny)*8
  * bytes with pitch = nx rounded up to 32 (about 116 000 nodes), is rejected
- * with LBM_ERR_ARG.  The first call on each device looks the array's address
- * up with cudaGetSymbolAddress, so make that first call before any stream
- * capture.  Every call shares the array: calls that overlap on the GPU race. */
+ * with LBM_ERR_ARG.  The first call in each device context (per device, and
+ * again after cudaDeviceReset) looks the array's address up with
+ * cudaGetSymbolAddress, so make that first call before any stream capture.
+ * Every call shares the array: calls that overlap on the GPU race. */
 #define LBM_NOALLOC_SCRATCH_BYTES ((size_t)8 << 20)
 int lbm_step_f64_noalloc(const lbm_geometry* g, const double* f, const double* rho, const double* u,
                          double omega, double* f_out, double* rho_out, double* u_out, int32_t flags,

@@ -290,7 +290,7 @@ def autotune(batch: Batch, candidates=None, steps: int = 6, warmup: int = 2):
     if candidates is None:
         npts = {"fx64": (1, 2), "f16": (2, 4, 8), "bf16": (2, 4, 8)}.get(batch.storage, (2, 4))
         candidates = [(p, t, b, r) for p in npts for t in (64, 128, 256) for b in (0, 8 * sms, ONE_TILE_PER_BLOCK)
-                      for r in (1, 2, 4, 8)]
+                      for r in (1, 2, 4, 8, 16)]
     best, results = None, []
     for cand in candidates:
         npt, threads, blocks = cand[:3]

@@ -11,10 +11,16 @@
 //
 // The array is a file-scope __device__ variable: every GPU that loads the
 // library holds LBM_NOALLOC_SCRATCH_BYTES of it until the process exits.  Its
-// address is looked up once per device with cudaGetSymbolAddress (host code
-// cannot use the symbol itself as a device pointer).  Every call on a device
-// shares the same array, so calls that overlap on the GPU (different streams,
-// or threads with no ordering between their streams) race on it.
+// address is looked up with cudaGetSymbolAddress (host code cannot use the
+// symbol itself as a device pointer) once per device context and cached under
+// the context's unique id, so a context created later on the same device
+// (after cudaDeviceReset, or another driver context made current) gets a
+// fresh lookup instead of an address that belonged to the old one.  Every call
+// in a context shares the same array, so calls that overlap on the GPU
+// (different streams, or threads with no ordering between their streams) race
+// on it.
+#include <cuda.h>
+
 #include <cstdio>
 #include <mutex>
 
@@ -25,32 +31,69 @@ namespace {
 // [9][ny][pitch] collided populations, then [3][ny] outlet column, float64
 __device__ __align__(256) unsigned char g_noalloc_scratch[LBM_NOALLOC_SCRATCH_BYTES];
 
-constexpr int kMaxDevices = 64;
+constexpr int kMaxContexts = 64;
 std::mutex g_mutex;
-void* g_scratch_addr[kMaxDevices] = {};
+unsigned long long g_ctx_id[kMaxContexts] = {};
+void* g_scratch_addr[kMaxContexts] = {};
+int g_next = 0;
 
-// Address of g_noalloc_scratch on the current device, looked up on first use.
+using CtxGetCurrent = CUresult (*)(CUcontext*);
+using CtxGetId = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrent g_get_current = nullptr;
+CtxGetId g_get_id = nullptr;
+
+int cuda_error(const char* what, cudaError_t e) {
+  char buf[256];
+  std::snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+  return lbm::set_error(LBM_ERR_CUDA, buf);
+}
+
+// unique id of the current driver context (0 when none is current yet);
+// the driver functions come through the runtime, so no driver library is linked
+int current_context_id(unsigned long long* id) {
+  if (g_get_current == nullptr || g_get_id == nullptr) {
+    cudaDriverEntryPointQueryResult q1, q2;
+    void* a = nullptr;
+    void* b = nullptr;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &a, 12000, cudaEnableDefault, &q1);
+    if (e == cudaSuccess) e = cudaGetDriverEntryPointByVersion("cuCtxGetId", &b, 12000, cudaEnableDefault, &q2);
+    if (e != cudaSuccess || q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !a || !b)
+      return lbm::set_error(LBM_ERR_CUDA, "cuCtxGetCurrent / cuCtxGetId not available from the driver");
+    g_get_current = reinterpret_cast<CtxGetCurrent>(a);
+    g_get_id = reinterpret_cast<CtxGetId>(b);
+  }
+  CUcontext ctx = nullptr;
+  if (g_get_current(&ctx) != CUDA_SUCCESS) return lbm::set_error(LBM_ERR_CUDA, "cuCtxGetCurrent failed");
+  *id = 0;
+  if (ctx != nullptr && g_get_id(ctx, id) != CUDA_SUCCESS) return lbm::set_error(LBM_ERR_CUDA, "cuCtxGetId failed");
+  return LBM_OK;
+}
+
+// Address of g_noalloc_scratch in the current context, looked up on first use
+// in that context.
 int scratch_address(void** out) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) {
-    char buf[256];
-    std::snprintf(buf, sizeof(buf), "cudaGetDevice: %s", cudaGetErrorString(e));
-    return lbm::set_error(LBM_ERR_CUDA, buf);
-  }
-  if (dev < 0 || dev >= kMaxDevices) return lbm::set_error(LBM_ERR_UNSUPPORTED, "device ordinal out of range");
   std::lock_guard<std::mutex> lock(g_mutex);
-  if (g_scratch_addr[dev] == nullptr) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || p == nullptr) {
-      char buf[256];
-      std::snprintf(buf, sizeof(buf), "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
-      return lbm::set_error(LBM_ERR_CUDA, buf);
-    }
-    g_scratch_addr[dev] = p;
+  unsigned long long id = 0;
+  if (int e = current_context_id(&id)) return e;
+  if (id != 0)
+    for (int k = 0; k < kMaxContexts; ++k)
+      if (g_ctx_id[k] == id) {
+        *out = g_scratch_addr[k];
+        return LBM_OK;
+      }
+  // first use in this context: the lookup also makes the device's primary
+  // context current when no context is yet
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || p == nullptr) return cuda_error("cudaGetSymbolAddress(scratch)", e);
+  if (id == 0)
+    if (int st = current_context_id(&id)) return st;
+  if (id != 0) {
+    g_ctx_id[g_next] = id;
+    g_scratch_addr[g_next] = p;
+    g_next = (g_next + 1) % kMaxContexts;
   }
-  *out = g_scratch_addr[dev];
+  *out = p;
   return LBM_OK;
 }
 

@@ -122,13 +122,16 @@ class ServingEngine:
     """Admits, batches and retires lattice solves on one GPU."""
 
     def __init__(self, storage="f16", hbm_budget=64 << 30, max_slots=128, tick_steps=500, npt=0, threads=0,
-                 blocks=0, device="cuda"):
+                 blocks=None, device="cuda"):
         self.storage = storage
         self.hbm_budget = int(hbm_budget)
         self.max_slots = max_slots
         self.tick_steps = tick_steps
         # one-row tiles: the batch changes every tick, and its tail (the last long
-        # requests) is a handful of lattices that need every tile they can get
+        # requests) is a handful of lattices that need every tile they can get;
+        # a plain grid of one tile per block by default
+        from .batch import ONE_TILE_PER_BLOCK
+        blocks = ONE_TILE_PER_BLOCK if blocks is None else blocks
         self.batch = Batch([], storage=storage, npt=npt, threads=threads, blocks=blocks, device=device, rows=1)
         self.live = []          # (Request, Member)
         self.used = 0
