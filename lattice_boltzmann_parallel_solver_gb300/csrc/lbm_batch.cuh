@@ -11,23 +11,14 @@
 
 namespace lbm {
 
-// Tiles are handed out in groups of `group` consecutive tiles (mostly of one
-// lattice), so the owner search and the staged entry are shared by the group;
-// groups are strided over the persistent grid.  The launcher makes groups
-// smaller when there are too few tiles to give every block several groups.
-constexpr int kTileGroup = 8;
-
-// Registers (measured on the 256-lattice sweep): the 16-bit bodies run fastest
-// at 768 threads per SM (up to 85 registers: no spills at 4 nodes per thread;
-// the loop state that the persistent grid keeps across the body spills under a
-// 64-register cap, 92 against 106 GLUPS); the boundary-free fixed-point body at
-// 1024 threads, as in the single-lattice kernel; with every boundary form
-// compiled in, 768.
+// Registers: the boundary-free 16-bit bodies and the one-node fixed-point body
+// run at 1024 threads per SM (64 registers; the plain grid and the span walk
+// keep little state across the body, 44 bytes of spill at 4 nodes per thread),
+// the bodies with the boundary sources inside at 768; float32 at 2 nodes per
+// thread without sources at 1024.
 template <int STORE, int NPT, int THREADS, bool HAS_BC>
 constexpr int batch_min_blocks() {
-  if constexpr (STORE == LBM_STORE_F16S || STORE == LBM_STORE_BF16S)
-    return 768 / THREADS;
-  else if constexpr (STORE == LBM_STORE_FX64 && NPT == 1)
+  if constexpr (STORE == LBM_STORE_F16S || STORE == LBM_STORE_BF16S || (STORE == LBM_STORE_FX64 && NPT == 1))
     return (HAS_BC ? 768 : 1024) / THREADS;
   else if constexpr (!HAS_BC && STORE == LBM_STORE_F32 && NPT <= 2)
     return 1024 / THREADS;
@@ -129,51 +120,47 @@ __device__ __forceinline__ void batch_tile(const BatchEntry& e, int local, int g
   }
 }
 
+// The persistent form: block b walks the contiguous span of tiles
+// [b T / B, (b + 1) T / B) (T tiles, B blocks), so consecutive tiles mostly
+// belong to one lattice: the owner search and the entry staging happen once per
+// lattice the span touches, not once per tile, and the spans differ by at most
+// one tile (no tail of partly filled waves).
 template <int STORE, int NPT, int THREADS, bool HAS_BC>
 __global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS, HAS_BC>())
     batch_kernel(const BatchEntry* __restrict__ tab, const int* __restrict__ tile_start, int n_inst,
-                 int total_tiles, const int* __restrict__ gbase, int k, int group) {
+                 int total_tiles, const int* __restrict__ gbase, int k) {
   // the current lattice's entry, staged in shared memory: the body reads its
   // parameters many times per tile, and in global memory the streaming
   // population traffic would evict them from L1
   __shared__ __align__(16) unsigned char ebuf[sizeof(BatchEntry)];
   const BatchEntry& e = *reinterpret_cast<const BatchEntry*>(ebuf);
-  int staged = -1;
+  const int per = total_tiles / (int)gridDim.x, extra = total_tiles % (int)gridDim.x;
+  const int b = (int)blockIdx.x;
+  const int t0 = b * per + min(b, extra), t1 = t0 + per + (b < extra ? 1 : 0);
+  if (t0 >= t1) return;
   const int g = *gbase + k;
-  const int groups = (total_tiles + group - 1) / group;
-  for (int grp = blockIdx.x; grp < groups; grp += gridDim.x) {
-    const int t0 = grp * group, t1 = min(total_tiles, t0 + group);
-    int lo = owner_of(tile_start, n_inst, t0);
-    int next = lo + 1 < n_inst ? __ldg(tile_start + lo + 1) : total_tiles;
-    for (int tile = t0; tile < t1; ++tile) {
-      while (tile >= next) {
+  int lo = owner_of(tile_start, n_inst, t0);
+  int first = __ldg(tile_start + lo);
+  int next = lo + 1 < n_inst ? __ldg(tile_start + lo + 1) : total_tiles;
+  stage_entry<THREADS, HAS_BC>(tab, lo, ebuf);
+  for (int tile = t0; tile < t1; ++tile) {
+    if (tile >= next) {
+      do {
         ++lo;
+        first = next;
         next = lo + 1 < n_inst ? __ldg(tile_start + lo + 1) : total_tiles;
-      }
-      if (lo != staged) {
-        stage_entry<THREADS, HAS_BC>(tab, lo, ebuf);
-        staged = lo;
-      }
-      if (g < e.s0 || g >= e.s_end) continue;
-      batch_tile<STORE, NPT, THREADS, HAS_BC>(e, tile - __ldg(tile_start + lo), g);
+      } while (tile >= next);
+      stage_entry<THREADS, HAS_BC>(tab, lo, ebuf);
     }
+    if (g >= e.s0 && g < e.s_end) batch_tile<STORE, NPT, THREADS, HAS_BC>(e, tile - first, g);
   }
 }
 
-// The plain-grid form (one tile per block, block b = tile b): no loop state
-// is kept across the body, so the 16-bit bodies fit 1024 threads per SM.  The
-// block copies the lattices' tile starts into shared memory (one round trip)
-// and finds its lattice there, instead of a search through global memory
-// (a dependent L2 round trip per halving).
+// The plain-grid form (one tile per block, block b = tile b).  The block
+// copies the lattices' tile starts into shared memory (one round trip) and
+// finds its lattice there, instead of a search through global memory (a
+// dependent L2 round trip per halving).
 constexpr int kStartSmem = 512;
-
-template <int STORE, int NPT, int THREADS, bool HAS_BC>
-constexpr int batch_grid_min_blocks() {
-  if constexpr (STORE == LBM_STORE_F16S || STORE == LBM_STORE_BF16S || (STORE == LBM_STORE_FX64 && NPT == 1))
-    return (HAS_BC ? 768 : 1024) / THREADS;
-  else
-    return batch_min_blocks<STORE, NPT, THREADS, HAS_BC>();
-}
 
 // owner_of for a whole block: the start list is copied into shared memory
 // (one round trip) and searched there when it has at most kStartSmem entries
@@ -193,7 +180,7 @@ __device__ __forceinline__ int owner_of_staged(const int* __restrict__ start, in
 }
 
 template <int STORE, int NPT, int THREADS, bool HAS_BC>
-__global__ void __launch_bounds__(THREADS, batch_grid_min_blocks<STORE, NPT, THREADS, HAS_BC>())
+__global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS, HAS_BC>())
     batch_grid_kernel(const BatchEntry* __restrict__ tab, const int* __restrict__ tile_start, int n_inst,
                       const int* __restrict__ gbase, int k) {
   __shared__ __align__(16) unsigned char ebuf[sizeof(BatchEntry)];
@@ -292,18 +279,17 @@ inline int launch_batch(const void* table, int n, int tiles, int bc_chunks, int*
     }
     blocks = fill;
   }
-  // groups of up to kTileGroup tiles, but at least two groups per block; a
-  // grid of more than half the tile count is a plain grid of one tile per block
+  // a grid of more than half the tile count is a plain grid of one tile per
+  // block; otherwise persistent blocks walk contiguous spans of tiles
   const bool plain = (int64_t)blocks * 2 > (int64_t)tiles;
-  const int group = (int)std::max<int64_t>(1, std::min<int64_t>(kTileGroup, (int64_t)tiles / (2 * (int64_t)blocks)));
-  blocks = std::min(blocks, std::max(1, (tiles + group - 1) / group));
+  blocks = std::min(blocks, std::max(1, tiles));
   for (int k = 0; k < nsteps; ++k) {
     if (plain && tiles > 0) {
       batch_grid_kernel<STORE, NPT, THREADS, HAS_BC><<<tiles, THREADS, 0, s>>>(tab, start, n, gbase, k);
       count_launch();
       if (int e = check_launch("batch_grid_kernel")) return e;
     } else {
-      batch_kernel<STORE, NPT, THREADS, HAS_BC><<<blocks, THREADS, 0, s>>>(tab, start, n, tiles, gbase, k, group);
+      batch_kernel<STORE, NPT, THREADS, HAS_BC><<<blocks, THREADS, 0, s>>>(tab, start, n, tiles, gbase, k);
       count_launch();
       if (int e = check_launch("batch_kernel")) return e;
     }
