@@ -440,9 +440,10 @@ def reference_arm(args):
     core, each stepping its own cavity sample; aggregate MLUPS."""
     import multiprocessing as mp
     cores = os.cpu_count() or 1
-    # per-process sample side: large enough to leave the caches, small enough
-    # that the whole --steps run stays within a few minutes
-    n = 512 if args.steps <= 600 else (256 if args.steps <= 3000 else 128)
+    # per-process sample side: the smallest cavity of the bandwidth benchmark
+    # (1024^2) for short runs, smaller ones so that the whole --steps run stays
+    # within a few minutes
+    n = 1024 if args.steps + args.warmup <= 100 else (512 if args.steps <= 600 else (256 if args.steps <= 3000 else 128))
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
         pool.map(_cpu_worker, [(64, 1, 0)] * cores)

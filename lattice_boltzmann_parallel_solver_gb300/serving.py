@@ -68,16 +68,11 @@ def _rest_state(nx, ny, device="cuda"):
             torch.zeros((nx, ny, 2), dtype=torch.float64, device=device))
 
 
-def request_mix(n, rate=50.0, seed=7, step_range=(1000, 50000), kinds=("couette", "poiseuille", "von_karman"),
-                lazy=False):
-    """Seeded Poisson arrivals (mean ``rate`` per second) of mixed requests:
-    Couette (moving top wall u_w in [0.01, 0.1], ny in [32, 512], nx = ny),
-    pressure-driven Poiseuille (delta rho log-uniform in [1e-4, 1e-2], nx x ny
-    up to 2048 x 512) and the von Karman channel (420 x 180, Re 100).  The
-    arrival gaps are rate-scaled draws of one seeded stream, so the same seed
-    gives the same requests (kinds, sizes, budgets) at every rate.  With ``lazy``
-    the initial states are built on the device at admission (long streams
-    would not fit the host memory up front)."""
+def request_stream(n, rate=50.0, seed=7, step_range=(1000, 50000), kinds=("couette", "poiseuille", "von_karman")):
+    """The seeded draws behind ``request_mix``, host only: per request (rid,
+    arrival, kind, steps, nx, ny, params).  The arrival gaps are rate-scaled
+    draws of one seeded stream, so the same seed gives the same requests
+    (kinds, sizes, budgets) at every rate."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
@@ -87,24 +82,42 @@ def request_mix(n, rate=50.0, seed=7, step_range=(1000, 50000), kinds=("couette"
         steps = int(rng.integers(step_range[0], step_range[1] + 1))
         if kind == "couette":
             ny = int(rng.integers(32, 513))
-            nx = ny
-            uw = float(rng.uniform(0.01, 0.1))
-            bnd = BU.Boundary([BU.rigid_wall(_row(nx, ny, 0)),
-                               BU.moving_wall(_row(nx, ny, -1), np.array([uw, 0.0]), 1.0)])
-            req = Request(rid, kind, nx, ny, 1.0, steps, bnd, None, None, None, t, {"u_w": uw},
-                          init=lambda nx=nx, ny=ny: _rest_state(nx, ny))
+            out.append((rid, t, kind, steps, ny, ny, {"u_w": float(rng.uniform(0.01, 0.1))}))
         elif kind == "poiseuille":
             nx = int(rng.integers(64, 2049))
             ny = int(rng.integers(16, 513))
             drho = float(math.exp(rng.uniform(math.log(1e-4), math.log(1e-2))))
-            p_in, p_out = (1 + drho / 2) / 3, (1 - drho / 2) / 3
-            bnd = BU.poiseuille_flow_boundary_conditions(nx, ny, p_in, p_out)
-            req = Request(rid, kind, nx, ny, 1.5, steps, bnd, None, None, None, t, {"drho": drho},
+            out.append((rid, t, kind, steps, nx, ny, {"drho": drho}))
+        else:
+            out.append((rid, t, kind, steps, 420, 180, {"re": 100}))
+    return out
+
+
+def request_mix(n, rate=50.0, seed=7, step_range=(1000, 50000), kinds=("couette", "poiseuille", "von_karman"),
+                lazy=False):
+    """Seeded Poisson arrivals (mean ``rate`` per second) of mixed requests:
+    Couette (moving top wall u_w in [0.01, 0.1], ny in [32, 512], nx = ny),
+    pressure-driven Poiseuille (delta rho log-uniform in [1e-4, 1e-2], nx x ny
+    up to 2048 x 512) and the von Karman channel (420 x 180, Re 100); the same
+    requests at every rate (``request_stream``).  With ``lazy`` the initial
+    states are built on the device at admission (long streams would not fit
+    the host memory up front)."""
+    out = []
+    for rid, t, kind, steps, nx, ny, params in request_stream(n, rate, seed, step_range, kinds):
+        if kind == "couette":
+            bnd = BU.Boundary([BU.rigid_wall(_row(nx, ny, 0)),
+                               BU.moving_wall(_row(nx, ny, -1), np.array([params["u_w"], 0.0]), 1.0)])
+            req = Request(rid, kind, nx, ny, 1.0, steps, bnd, None, None, None, t, params,
+                          init=lambda nx=nx, ny=ny: _rest_state(nx, ny))
+        elif kind == "poiseuille":
+            d = params["drho"]
+            bnd = BU.poiseuille_flow_boundary_conditions(nx, ny, (1 + d / 2) / 3, (1 - d / 2) / 3)
+            req = Request(rid, kind, nx, ny, 1.5, steps, bnd, None, None, None, t, params,
                           init=lambda nx=nx, ny=ny: _rest_state(nx, ny))
         else:
             om = 1.0 / (3.0 * (0.1 * 40 / 100.0) + 0.5)
             bnd = BU.von_karman_boundary_conditions(420, 180, 1.0, 0.1, 40, walls=True, plate_offset=1)
-            req = Request(rid, kind, 420, 180, om, steps, bnd, None, None, None, t, {"re": 100},
+            req = Request(rid, kind, 420, 180, om, steps, bnd, None, None, None, t, params,
                           init=lambda rid=rid: S.von_karman_start(420, 180, 0.1, 1e-3, seed=rid))
         if not lazy:
             req.f0, req.rho0, req.u0 = req.init()
