@@ -55,7 +55,7 @@ class Batch:
     """A set of lattices sharing one storage type, advanced in lock step.
     Members can join (``add``) and leave (``remove``) between runs."""
 
-    def __init__(self, members=(), storage: str = "f16", npt: int = 0, threads: int = 0, blocks: int = 0,
+    def __init__(self, members=(), storage: str = "f16", npt: int = 0, threads: int = 0, blocks: int = None,
                  device: str = "cuda", stochastic: bool = None, rows: int = 0, inline_bc: bool | None = None):
         """Batches of at least 2^20 nodes take each step as a boundary-free
         launch over every node followed by a pass over the boundary nodes,
@@ -64,9 +64,12 @@ class Batch:
         ``npt``, ``threads`` and ``rows`` (nodes per thread, threads per tile,
         runs of ``threads`` chunks per tile) default to what ``autotune`` picks
         for such batches (``_default_shape``; for large mixed von Karman
-        batches 1 x 64 for fx64 with 4 runs, 4 x 64 for the 16-bit storages
-        with 2 runs; several runs only when the batch has enough of them to
-        keep every SM busy, 1 otherwise)."""
+        batches 1 x 64 for fx64 with 4 runs, 4 x 128 for the 16-bit storages
+        with 8 runs; several runs only when the batch has enough of them to
+        keep every SM busy, 1 otherwise).  ``blocks``: the default (None) is a
+        plain grid of one tile per block, 0 persistent blocks filling the GPU
+        that walk contiguous spans of tiles, any other number that many
+        persistent blocks."""
         A.require_cuda()
         self.stochastic = storage in ("f16", "bf16") if stochastic is None else bool(stochastic)
         self.storage = storage
@@ -78,7 +81,7 @@ class Batch:
         self._auto_shape = (not npt, not threads)
         self.npt, self.threads = int(npt), int(threads)
         self._default_shape(0)
-        self.blocks = blocks
+        self.blocks = ONE_TILE_PER_BLOCK if blocks is None else blocks
         self.rows = int(rows)           # runs per tile (0: chosen from the batch size)
         self.bc_chunks = -1             # boundary-node plan of the work table (-1: sources in the step)
         self.gbase = torch.zeros(1, dtype=torch.int32, device=self.device)
@@ -152,13 +155,12 @@ class Batch:
         if self._auto_shape[0]:
             self.npt = {"fx64": 1, "f64": 2, "f16": 4 if split else 2, "bf16": 4 if split else 2}.get(self.storage, 4)
         if self._auto_shape[1]:
-            self.threads = {"f16": 64 if split else 128, "bf16": 64 if split else 128,
-                            "fx64": 64 if split else 128}.get(self.storage, 128)
+            self.threads = {"fx64": 64 if split else 128}.get(self.storage, 128)
 
     def _rows(self) -> int:
         """Runs per tile (a run: ``threads`` consecutive chunks of ``npt``
         nodes, row by row): the given number, else (when the batch has at
-        least 64 runs per SM) 2 for the 16-bit storages and 4 for the others,
+        least 64 runs per SM) 8 for the 16-bit storages and 4 for the others,
         else 1."""
         if self.rows > 0:
             return self.rows
@@ -166,7 +168,7 @@ class Batch:
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
         if runs < 64 * sms:
             return 1
-        return 2 if self.storage in ("f16", "bf16") else 4
+        return 8 if self.storage in ("f16", "bf16") else 4
 
     def _build(self, with_probes=True):
         n = len(self.members)

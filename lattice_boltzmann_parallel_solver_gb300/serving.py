@@ -142,9 +142,7 @@ class ServingEngine:
         self.tick_steps = tick_steps
         # one-row tiles: the batch changes every tick, and its tail (the last long
         # requests) is a handful of lattices that need every tile they can get;
-        # a plain grid of one tile per block by default
-        from .batch import ONE_TILE_PER_BLOCK
-        blocks = ONE_TILE_PER_BLOCK if blocks is None else blocks
+        # a plain grid of one tile per block by default (blocks None)
         self.batch = Batch([], storage=storage, npt=npt, threads=threads, blocks=blocks, device=device, rows=1)
         self.live = []          # (Request, Member)
         self.used = 0

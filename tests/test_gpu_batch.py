@@ -160,6 +160,23 @@ def test_plain_edge_columns_equal_inline_sources(pkg, storage, probe):
     assert ta.shape[0] == 59 and torch.equal(ta, tb)
 
 
+@pytest.mark.parametrize("storage,inline", [("f16", False), ("fx64", False), ("f16", True)])
+def test_persistent_spans_equal_plain_grid(pkg, storage, inline):
+    """The persistent form (blocks walking contiguous spans of tiles, spans that
+    cross lattices) gives the same bits as the plain grid of one tile per block."""
+    from lattice_boltzmann_parallel_solver_gb300.batch import ONE_TILE_PER_BLOCK, Batch
+    npt = 1 if storage == "fx64" else 4
+    runs = []
+    for blocks in (ONE_TILE_PER_BLOCK, 0, 7):
+        ms = members(pkg, steps=(30, 17, 25, 30, 9))
+        b = Batch(ms, storage=storage, npt=npt, threads=64, rows=2, blocks=blocks, inline_bc=inline).start()
+        b.run()
+        runs.append([b.read(j)[0] for j in range(len(ms))])
+    for other in runs[1:]:
+        for x, y in zip(runs[0], other):
+            assert torch.equal(x, y)
+
+
 def test_batch_plan_follows_the_size(pkg):
     """Below 2^20 nodes in total a batch keeps the boundary sources inside one
     launch per step; from 2^20 it runs the boundary-free step and the pass."""
