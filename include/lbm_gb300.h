@@ -74,22 +74,17 @@ typedef struct lbm_geometry {
    * LBM_FLAG_BC_INLINE applies the sources inside the step. */
   const int32_t* bcnodes;
   int32_t n_bcnodes;
-  /* Plain inlet / outlet columns and wall rows (all zero: none).
-   * edge_inlet_desc is the descriptor of the nodes of column 0 that take only
-   * the inlet populations (all nine directions CONST from one constant set),
-   * edge_outlet_desc that of the nodes of column nx-1 that take only directions
-   * 3, 6, 7 from the outlet memory (the others stream), edge_bottom_desc /
-   * edge_top_desc that of the nodes of row 0 / ny-1 that take only directions
-   * 2, 5, 6 / 4, 7, 8 by bounce-back (rigid or moving wall; the others
-   * stream); each is set only when every node of its column or row has a
-   * descriptor.  The last n_bcnodes_edge entries of bcnodes are the nodes with
-   * one of these descriptors and no other of the four forms applying at them
-   * (the others, corners included, come first).  The batched step applies the
-   * forms inside its boundary-free launch, where a whole row or column costs a
-   * few extra loads per chunk, and passes over the other entries only. */
+  /* Plain inlet and outlet columns (all zero: none).  edge_inlet_desc is the
+   * descriptor of the nodes of column 0 that take only the inlet populations
+   * (all nine directions CONST from one constant set), edge_outlet_desc that
+   * of the nodes of column nx-1 that take only directions 3, 6, 7 from the
+   * outlet memory (the others stream); each is set only when every node of
+   * its column has a descriptor.  The last n_bcnodes_edge entries of bcnodes
+   * are the nodes with these two descriptors (the others come first).  The
+   * batched step applies them inside its boundary-free launch, where they cost
+   * no scattered column accesses, and passes over the other entries only. */
   uint32_t edge_inlet_desc, edge_outlet_desc;
   int32_t n_bcnodes_edge;
-  uint32_t edge_bottom_desc, edge_top_desc;
 } lbm_geometry;
 
 /* ---- storage / arithmetic of the resident state ------------------------- */

@@ -48,7 +48,6 @@ class Geometry(C.Structure):
         ("outlet", i32),
         ("bcnodes", vp), ("n_bcnodes", i32),
         ("edge_inlet_desc", C.c_uint32), ("edge_outlet_desc", C.c_uint32), ("n_bcnodes_edge", i32),
-        ("edge_bottom_desc", C.c_uint32), ("edge_top_desc", C.c_uint32),
     ]
 
 

@@ -4,7 +4,6 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
-#include <type_traits>
 
 #include "lbm_core.cuh"
 #include "lbm_fx.cuh"
@@ -26,13 +25,10 @@ struct GeoK {
   double cconst[LBM_MAX_SETS][9];
   const int32_t* bcnodes;
   int n_bcnodes;
-  // plain inlet / outlet columns and wall rows (lbm_geometry), the inlet's
-  // populations and the walls' bounce-back terms (directions 2, 5, 6 at the
-  // bottom, 4, 7, 8 at the top)
-  uint32_t edge_in_desc, edge_out_desc, edge_bot_desc, edge_top_desc;
+  // plain inlet / outlet columns (lbm_geometry), and the inlet's populations
+  uint32_t edge_in_desc, edge_out_desc;
   int n_bcnodes_edge;
   double edge_in_f[9];
-  double edge_bot_k[3], edge_top_k[3];
 };
 
 struct View {
@@ -78,13 +74,10 @@ __device__ __forceinline__ uint32_t launch_seed(const KParams& P) {
   return P.step_dev != nullptr ? hash32(P.seed + (uint32_t)__ldg(P.step_dev)) : P.seed;
 }
 
-// a node the body applies as a plain edge node itself (edges on): exactly one
-// of the plain column / row forms applies at it and it has that descriptor
+// a node the body applies as a plain inlet / outlet node itself (edges on)
 __device__ __forceinline__ bool plain_edge_node(const KParams& P, int x, int y) {
-  const uint32_t col = x == 0 ? P.g.edge_in_desc : (x == P.g.nx - 1 ? P.g.edge_out_desc : 0u);
-  const uint32_t row = y == 0 ? P.g.edge_bot_desc : (y == P.g.ny - 1 ? P.g.edge_top_desc : 0u);
-  if ((col != 0u) == (row != 0u)) return false;
-  return __ldg(P.g.desc + y * P.g.nx + x) == (col | row);
+  const uint32_t want = x == 0 ? P.g.edge_in_desc : (x == P.g.nx - 1 ? P.g.edge_out_desc : 0u);
+  return want != 0u && __ldg(P.g.desc + y * P.g.nx + x) == want;
 }
 
 // skip_bc: a body without its boundary block leaves the probe of a node that
@@ -222,30 +215,6 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
         f[7][k] = k == kl ? a7 : f[7][k];
       }
     }
-    // the plain wall rows: bounce-back at the node itself, minus the moving-wall
-    // term (destination directions fixed at compile time, so f stays in registers)
-    auto wall_row = [&](const double* kk, auto d0, auto d1, auto d2) {
-      constexpr int dst[3] = {decltype(d0)::value, decltype(d1)::value, decltype(d2)::value};
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        const int src = opp(dst[j]);
-        const R kj = (R)kk[j] * kS;
-        if constexpr (NPT == 1) {
-          f[dst[j]][0] = ld_work(pin + src * plane + r0 + x0, src) - kj;
-        } else {
-          T raw[NPT];
-          ld_vec<T, NPT>(pin + src * plane + r0 + x0, raw);
-#pragma unroll
-          for (int k = 0; k < NPT; ++k) f[dst[j]][k] = work_of_raw(raw[k], src) - kj;
-        }
-      }
-    };
-    if (y == 0 && P.g.edge_bot_desc != 0u)
-      wall_row(P.g.edge_bot_k, std::integral_constant<int, 2>{}, std::integral_constant<int, 5>{},
-               std::integral_constant<int, 6>{});
-    else if (y == ny - 1 && P.g.edge_top_desc != 0u)
-      wall_row(P.g.edge_top_k, std::integral_constant<int, 4>{}, std::integral_constant<int, 7>{},
-               std::integral_constant<int, 8>{});
   }
 
   if (has_bc) {
@@ -504,30 +473,6 @@ __device__ __forceinline__ void fused_fx_body(const KParams& P, const void* pop_
         f[7][k] = k == kl ? a7 : f[7][k];
       }
     }
-    // the plain wall rows: bounce-back at the node itself, minus the moving-wall
-    // term (destination directions fixed at compile time, so f stays in registers)
-    auto wall_row = [&](const double* kk, auto d0, auto d1, auto d2) {
-      constexpr int dst[3] = {decltype(d0)::value, decltype(d1)::value, decltype(d2)::value};
-#pragma unroll
-      for (int j = 0; j < 3; ++j) {
-        const int src = opp(dst[j]);
-        const T kj = fx::round_scaled(kk[j], fx::kS);
-        if constexpr (NPT == 1) {
-          f[dst[j]][0] = __ldg(pin + src * plane + r0 + x0) - kj;
-        } else {
-          T v[NPT];
-          ld_vec<T, NPT>(pin + src * plane + r0 + x0, v);
-#pragma unroll
-          for (int k = 0; k < NPT; ++k) f[dst[j]][k] = v[k] - kj;
-        }
-      }
-    };
-    if (y == 0 && P.g.edge_bot_desc != 0u)
-      wall_row(P.g.edge_bot_k, std::integral_constant<int, 2>{}, std::integral_constant<int, 5>{},
-               std::integral_constant<int, 6>{});
-    else if (y == ny - 1 && P.g.edge_top_desc != 0u)
-      wall_row(P.g.edge_top_k, std::integral_constant<int, 4>{}, std::integral_constant<int, 7>{},
-               std::integral_constant<int, 8>{});
   }
 
   if (has_bc) {
@@ -705,26 +650,13 @@ inline bool to_geok(const lbm_geometry* g, GeoK& k) {
     return set_error(LBM_ERR_ARG, "edge_inlet_desc is not an all-CONST descriptor"), false;
   if (g->edge_outlet_desc != 0u && (g->edge_outlet_desc & 0x3FFFFu) != 0xF0C0u)
     return set_error(LBM_ERR_ARG, "edge_outlet_desc is not the plain outlet descriptor"), false;
-  if (g->edge_bottom_desc != 0u && (g->edge_bottom_desc & 0x3FFFFu) != 0x1410u)
-    return set_error(LBM_ERR_ARG, "edge_bottom_desc is not the plain bottom-wall descriptor"), false;
-  if (g->edge_top_desc != 0u && (g->edge_top_desc & 0x3FFFFu) != 0x14100u)
-    return set_error(LBM_ERR_ARG, "edge_top_desc is not the plain top-wall descriptor"), false;
   if (k.bcmask != nullptr) {
-    k.edge_in_desc = g->nx >= 2 ? g->edge_inlet_desc : 0u;
+    k.edge_in_desc = g->edge_inlet_desc;
     k.edge_out_desc = g->nx >= 2 ? g->edge_outlet_desc : 0u;
-    k.edge_bot_desc = g->ny >= 2 ? g->edge_bottom_desc : 0u;
-    k.edge_top_desc = g->ny >= 2 ? g->edge_top_desc : 0u;
     k.n_bcnodes_edge = g->n_bcnodes_edge;
     const int cs = (int)((g->edge_inlet_desc >> LBM_DESC_CSET_SHIFT) & 15u);
     if (k.edge_in_desc != 0u)
       for (int i = 0; i < 9; ++i) k.edge_in_f[i] = g->cconst[cs][i];
-    const int kb = (int)((g->edge_bottom_desc >> LBM_DESC_KSET_SHIFT) & 15u);
-    const int kt = (int)((g->edge_top_desc >> LBM_DESC_KSET_SHIFT) & 15u);
-    const int bot[3] = {2, 5, 6}, top[3] = {4, 7, 8};
-    for (int j = 0; j < 3; ++j) {
-      k.edge_bot_k[j] = k.edge_bot_desc != 0u ? g->kconst[kb][bot[j]] : 0.0;
-      k.edge_top_k[j] = k.edge_top_desc != 0u ? g->kconst[kt][top[j]] : 0.0;
-    }
   }
   return true;
 }

@@ -79,11 +79,10 @@ class CompiledGeometry:
             self.bcmask = torch.from_numpy(np.ascontiguousarray(bcmask)).to(device)
             g.desc = self.desc.data_ptr()
             g.bcmask = self.bcmask.data_ptr()
-            # plain inlet / outlet columns and wall rows: the batched boundary-free
-            # step applies them itself, its boundary-node pass skips them
+            # plain inlet / outlet columns: the batched boundary-free step applies
+            # them itself, its boundary-node pass skips them
             edge = np.zeros((nx, ny), dtype=bool)
-            (g.edge_inlet_desc, g.edge_outlet_desc, g.edge_bottom_desc,
-             g.edge_top_desc) = self._edge_desc(src, desc, special, edge)
+            g.edge_inlet_desc, g.edge_outlet_desc = self._edge_desc(src, desc, special, edge)
             # linear indices y*nx + x of the boundary nodes, for the boundary-node
             # pass: the other boundary nodes first, then the plain edge nodes
             core = np.flatnonzero((special & ~edge).T.reshape(-1))
@@ -114,47 +113,28 @@ class CompiledGeometry:
 
     @staticmethod
     def _edge_desc(src, desc, special, edge):
-        """(inlet, outlet, bottom, top) descriptors of the plain edge nodes, 0 for
-        none; marks those nodes in ``edge``.  Plain inlet: all nine sources CONST
-        (column 0); plain outlet: directions 3, 6, 7 OUTLET and the others PULL
-        (column nx-1); plain bottom / top wall: directions 2, 5, 6 / 4, 7, 8
-        BOUNCE and the others PULL (row 0 / ny-1); of each kind the most common
-        descriptor.  A column or row qualifies only when every node of it has a
-        descriptor, so that a kernel may apply the form to all of it and leave
-        the other nodes to the pass.  A node counts as plain only where one form
-        alone applies (the corners where a row meets a column stay in the pass)."""
-        nx, ny = src.shape[0], src.shape[1]
-        B, O, C, P_ = BOUNCE, OUTLET, CONST, PULL
-        forms = [  # (axis 0 = column x / 1 = row y, index, sources of the nine directions)
-            (0, 0, [C] * 9),
-            (0, nx - 1, [O if i in (3, 6, 7) else P_ for i in range(9)]),
-            (1, 0, [B if i in (2, 5, 6) else P_ for i in range(9)]),
-            (1, ny - 1, [B if i in (4, 7, 8) else P_ for i in range(9)]),
-        ]
-        out, applied, plain_of = [], np.zeros((nx, ny), dtype=np.int32), []
-        for axis, idx, want in forms:
-            line = (slice(idx, idx + 1), slice(None)) if axis == 0 else (slice(None), slice(idx, idx + 1))
-            n_other = ny if axis == 1 else nx
-            if n_other < 2 or not special[line].all():
+        """(inlet, outlet) descriptors of the plain edge nodes, 0 for none; marks
+        those nodes in ``edge``.  Plain inlet: all nine sources CONST (the most
+        common such descriptor of column 0); plain outlet: directions 3, 6, 7
+        OUTLET and the others PULL (column nx-1).  A column qualifies only when
+        every node of it has a descriptor, so that a kernel may apply the form
+        to the whole column and leave the other nodes to the pass."""
+        nx = src.shape[0]
+        out = []
+        for x, want in ((0, np.full(9, CONST)),
+                        (nx - 1, np.array([OUTLET if i in (3, 6, 7) else PULL for i in range(9)]))):
+            if nx < 2 or not special[x, :].all():
                 out.append(0)
-                plain_of.append(None)
                 continue
-            plain = (src[line] == np.array(want, dtype=np.uint32)).all(axis=-1)
+            plain = (src[x] == want.astype(np.uint32)).all(axis=-1)
             if not plain.any():
                 out.append(0)
-                plain_of.append(None)
                 continue
-            vals, counts = np.unique(desc[line][plain], return_counts=True)
+            vals, counts = np.unique(desc[x, plain], return_counts=True)
             d = int(vals[np.argmax(counts)])
-            m = np.zeros((nx, ny), dtype=bool)
-            m[line] = plain & (desc[line] == d)
-            applied[line] += 1
+            edge[x, :] |= plain & (desc[x, :] == d)
             out.append(d)
-            plain_of.append(m)
-        for m in plain_of:
-            if m is not None:
-                edge |= m & (applied == 1)
-        return tuple(out)
+        return out[0], out[1]
 
     @property
     def ref(self):

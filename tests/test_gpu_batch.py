@@ -135,15 +135,13 @@ def test_boundary_node_pass_equals_inline_sources(pkg, storage):
 
 
 @pytest.mark.parametrize("storage", ["fx64", "f16", "f32"])
-@pytest.mark.parametrize("probe", [(202, 30), (0, 0), (202, 61), (0, 17), (1, 17), (201, 30), (100, 0), (100, 61),
-                                   (1, 0), (201, 61), (51, 0)])
+@pytest.mark.parametrize("probe", [(202, 30), (0, 0), (202, 61), (0, 17), (1, 17), (201, 30)])
 def test_plain_edge_columns_equal_inline_sources(pkg, storage, probe):
     """The batched boundary-free step applies the plain inlet and outlet columns
-    and the plain wall rows itself and the pass skips them: bit-identical to the
-    sources inside the step, with the probe on a plain outlet node, on the
-    corners where the walls meet the inlet / outlet (nodes the pass
-    recomputes), on a plain inlet node, next to both columns, on plain bottom
-    and top wall nodes and next to the corners."""
+    itself and the pass skips them: bit-identical to the sources inside the
+    step, with the probe on a plain outlet node, on the corners where the walls
+    override the inlet / outlet (nodes the pass recomputes), on a plain inlet
+    node and next to both columns."""
     from lattice_boltzmann_parallel_solver_gb300.batch import Batch
     npt = {"fx64": 1, "f32": 2}.get(storage, 4)
     runs = []
@@ -153,8 +151,7 @@ def test_plain_edge_columns_equal_inline_sources(pkg, storage, probe):
         b = Batch(ms, storage=storage, npt=npt, threads=64, rows=2, inline_bc=inline).start()
         if not inline:
             g = ms[0].geo.struct
-            assert g.n_bcnodes_edge == 2 * (62 - 2) + 2 * (203 - 2)
-            assert g.edge_inlet_desc and g.edge_outlet_desc and g.edge_bottom_desc and g.edge_top_desc
+            assert g.n_bcnodes_edge == 2 * (62 - 2) and g.edge_inlet_desc and g.edge_outlet_desc
         b.run()
         runs.append(b)
     a, b = runs
