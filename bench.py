@@ -333,11 +333,12 @@ def bench_serve(P, n=60, rates=None):
                         "each offered Poisson rate, HBM budget 64 GB" % n, "results": out}
 
 
-def bench_serve_sweep(P, window_s=60.0):
+def bench_serve_sweep(P, window_s=60.0, rates=None):
     """Offered load swept up to and beyond each storage's capacity, every rate
     with at least ``window_s`` seconds of arrivals (n = rate x window requests,
     a prefix of one seeded stream): solves/s, p50 and p99 latency per rate."""
-    rates = {"f16": (4.0, 8.0, 12.0, 16.0, 20.0), "fx64": (1.5, 3.0, 4.5, 6.0), "f64": (0.5, 1.0, 1.5, 2.0)}
+    rates = rates or {"f16": (4.0, 8.0, 12.0, 16.0, 20.0, 24.0), "fx64": (1.5, 3.0, 4.5, 6.0, 8.0),
+                      "f64": (0.5, 1.0, 1.5, 2.0)}
     out = {}
     for storage, rs in rates.items():
         out[storage] = []

@@ -3,9 +3,10 @@
 Requests (a boundary composition, an initial state and a step budget) arrive
 over time.  At every tick the engine admits waiting requests while their
 device state fits the HBM budget and a slot is free, advances every live
-request together by up to ``tick_steps`` steps in batched launches (one
-launch per step covering all of them), and retires the requests whose budget
-is spent: their final moments are read back and their memory is freed.
+request together by ``tick_steps`` steps in batched launches (one launch per
+step covering all of them; a request whose budget ends inside the tick stops
+at its last step), and retires the requests whose budget is spent: their
+final moments are read back and their memory is freed.
 Requests that arrive while others are on the GPU join at the next tick, so
 their work overlaps on the device.  A request's result does not depend on
 what it shared the GPU with: every lattice is updated by the same kernel and
@@ -140,10 +141,11 @@ class ServingEngine:
         self.hbm_budget = int(hbm_budget)
         self.max_slots = max_slots
         self.tick_steps = tick_steps
-        # one-row tiles: the batch changes every tick, and its tail (the last long
-        # requests) is a handful of lattices that need every tile they can get;
-        # a plain grid of one tile per block by default (blocks None)
-        self.batch = Batch([], storage=storage, npt=npt, threads=threads, blocks=blocks, device=device, rows=1)
+        # a plain grid of one tile per block by default (blocks None); runs per
+        # tile chosen by the batch size each time the table is rebuilt (one run
+        # per tile for the small batches of the tail, whose few lattices need
+        # every tile they can get)
+        self.batch = Batch([], storage=storage, npt=npt, threads=threads, blocks=blocks, device=device)
         self.live = []          # (Request, Member)
         self.used = 0
         self.stats = {"ticks": 0, "max_live": 0, "steps": 0}
@@ -186,7 +188,11 @@ class ServingEngine:
                 if waiting:
                     raise RuntimeError("request %d does not fit the HBM budget" % waiting[0].rid)
                 continue
-            left = min(m.s0 + m.steps - 1 - b.g for _, m in self.live)
+            # full ticks: a request whose budget ends inside the tick stops there
+            # by itself (the batched step skips a lattice outside its window) and
+            # retires at the tick's end, so one short request does not cut every
+            # tick short
+            left = max(m.s0 + m.steps - 1 - b.g for _, m in self.live)
             n = max(0, min(self.tick_steps, left))
             b.run(n)
             self.stats["ticks"] += 1
