@@ -42,6 +42,7 @@ class Request:
     params: dict = field(default_factory=dict)
     init: object = None           # () -> (f0, rho0, u0): the initial state built on demand
     # filled in by the engine
+    prepared: tuple = None        # the initial state on the device, built while the GPU runs a tick
     admitted: float = None
     finished: float = None
     rho: torch.Tensor = None
@@ -149,6 +150,23 @@ class ServingEngine:
         self.live = []          # (Request, Member)
         self.used = 0
         self.stats = {"ticks": 0, "max_live": 0, "steps": 0}
+        # host work for the next requests (boundary compile, initial state) runs
+        # while the GPU runs a tick; its copies and kernels go on this stream
+        self.side = torch.cuda.Stream(device=self.batch.device)
+
+    def _prepare(self, reqs):
+        """Compile the boundary descriptor and build the initial state on the
+        device for requests about to be admitted, on the side stream."""
+        for r in reqs:
+            if r.prepared is not None:
+                continue
+            with torch.cuda.stream(self.side):
+                r.boundary.geometry(r.nx, r.ny)
+                state = r.initial_state()
+                r.prepared = tuple(None if t is None else
+                                   (t if isinstance(t, torch.Tensor) else torch.from_numpy(np.asarray(t))).to(
+                                       self.batch.device, non_blocking=False)
+                                   for t in state)
 
     def state_bytes(self, req):
         per = {"fx64": 8, "f64": 8, "f32": 4, "f16": 2, "bf16": 2}[self.storage]
@@ -173,14 +191,22 @@ class ServingEngine:
             while i < len(pending) and (pending[i].arrival <= now or not realtime):
                 waiting.append(pending[i])
                 i += 1
+            main = torch.cuda.current_stream(b.device)
             while waiting and len(self.live) < self.max_slots and \
                     self.used + self.state_bytes(waiting[0]) <= self.hbm_budget:
                 r = waiting.pop(0)
                 r.admitted = now
-                f0, rho0, u0 = r.initial_state()
+                self._prepare([r])
+                main.wait_stream(self.side)
+                f0, rho0, u0 = r.prepared
                 m = b.add(Member(r.nx, r.ny, r.omega, r.boundary, steps=r.steps, f0=f0, rho0=rho0, u0=u0))
-                # the first step has consumed the initial state
+                # the first step has consumed the initial state (its memory, from
+                # the side stream's pool, is not reused before that step has run)
+                for t in r.prepared:
+                    if t is not None:
+                        t.record_stream(main)
                 m.f0 = m.rho0 = m.u0 = None
+                r.prepared = None
                 del f0, rho0, u0
                 self.live.append((r, m))
                 self.used += self.state_bytes(r)
@@ -198,6 +224,13 @@ class ServingEngine:
             self.stats["ticks"] += 1
             self.stats["steps"] += n
             self.stats["max_live"] = max(self.stats["max_live"], len(self.live))
+            # while the tick runs: take in the arrivals and prepare the requests
+            # that the next admissions will take
+            now = time.perf_counter() - t0
+            while i < len(pending) and (pending[i].arrival <= now or not realtime):
+                waiting.append(pending[i])
+                i += 1
+            self._prepare(waiting[:max(0, self.max_slots - len(self.live)) + 4])
             finished = [(r, m) for r, m in self.live if b.done(m)]
             if finished:
                 for r, m in finished:
