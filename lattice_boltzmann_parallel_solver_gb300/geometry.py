@@ -36,23 +36,35 @@ def dir_mask(dirs) -> int:
 
 
 class CompiledGeometry:
-    """Device-resident descriptor of one boundary composition on an nx x ny lattice."""
+    """Device-resident descriptor of one boundary composition on an nx x ny lattice.
+
+    The compile works on the nodes that some source writes (gathered from the
+    masks), not on dense per-direction arrays of the whole lattice, so its
+    host cost grows with the boundary, not with nx * ny (a 2048 x 512
+    Poiseuille lattice: a 4 MB descriptor array and two rows of sources)."""
 
     def __init__(self, nx: int, ny: int, sources=(), pressure=None, device="cuda"):
         self.nx, self.ny = int(nx), int(ny)
-        src = np.zeros((nx, ny, 9), dtype=np.uint32)
-        kv = np.zeros((nx, ny, 9))
-        cv = np.zeros((nx, ny, 9))
+        # linear indices y * nx + x of the nodes each source writes
+        lins = []
         for mask, i, kind, value in sources:
             mask = np.asarray(mask, dtype=bool)
             assert mask.shape == (nx, ny), "boundary mask shape %s does not match the lattice %s" % (
                 mask.shape, (nx, ny))
-            src[mask, i] = kind
-            kv[mask, i] = value if kind == BOUNCE else 0.0
-            cv[mask, i] = value if kind == CONST else 0.0
-        special = (src != PULL).any(axis=-1)
-        self.n_special = int(special.sum())
-        outlet_cols = np.nonzero((src == OUTLET).any(axis=(1, 2)))[0]
+            lins.append(np.flatnonzero(mask.T))
+        nodes = np.unique(np.concatenate(lins)) if lins else np.zeros(0, dtype=np.int64)
+        src = np.zeros((nodes.size, 9), dtype=np.uint32)
+        kv = np.zeros((nodes.size, 9))
+        cv = np.zeros((nodes.size, 9))
+        for (mask, i, kind, value), lin in zip(sources, lins):
+            pos = np.searchsorted(nodes, lin)
+            src[pos, i] = kind
+            kv[pos, i] = value if kind == BOUNCE else 0.0
+            cv[pos, i] = value if kind == CONST else 0.0
+        keep = (src != PULL).any(axis=-1)
+        nodes, src, kv, cv = nodes[keep], src[keep], kv[keep], cv[keep]
+        self.n_special = int(nodes.size)
+        outlet_cols = np.unique(nodes[(src == OUTLET).any(axis=-1)] % nx)
         self.outlet = bool(outlet_cols.size)
         # the fused kernels keep the outlet's previous populations for column nx-1 only
         self.fusable = bool(np.all(outlet_cols == nx - 1))
@@ -61,44 +73,43 @@ class CompiledGeometry:
         g.nx, g.ny = self.nx, self.ny
         g.outlet = int(self.outlet)
         if self.n_special:
-            ktab, kidx = np.unique(kv[special], axis=0, return_inverse=True)
-            ctab, cidx = np.unique(cv[special], axis=0, return_inverse=True)
+            ktab, kidx = np.unique(kv, axis=0, return_inverse=True)
+            ctab, cidx = np.unique(cv, axis=0, return_inverse=True)
             if len(ktab) > _lib.MAX_SETS or len(ctab) > _lib.MAX_SETS:
                 raise NotImplementedError("more than %d distinct boundary constant sets" % _lib.MAX_SETS)
-            desc = np.zeros((nx, ny), dtype=np.uint32)
+            packed = np.zeros(nodes.size, dtype=np.uint32)
             for i in range(9):
-                desc |= src[..., i] << np.uint32(2 * i)
-            desc[special] |= (kidx.reshape(-1).astype(np.uint32) << np.uint32(_lib.KSET_SHIFT)) | \
+                packed |= src[:, i] << np.uint32(2 * i)
+            packed |= (kidx.reshape(-1).astype(np.uint32) << np.uint32(_lib.KSET_SHIFT)) | \
                 (cidx.reshape(-1).astype(np.uint32) << np.uint32(_lib.CSET_SHIFT))
+            desc = np.zeros(ny * nx, dtype=np.uint32)
+            desc[nodes] = packed
             words = (nx + 31) // 32
-            bits = np.zeros((ny, words * 32), dtype=np.uint64)
-            bits[:, :nx] = special.T
-            bits = bits.reshape(ny, words, 32)
-            bcmask = (bits << np.arange(32, dtype=np.uint64)).sum(axis=-1).astype(np.uint32)
-            self.desc = torch.from_numpy(np.ascontiguousarray(desc.T)).to(device)
-            self.bcmask = torch.from_numpy(np.ascontiguousarray(bcmask)).to(device)
+            x, y = nodes % nx, nodes // nx
+            bcmask = np.zeros(ny * words, dtype=np.uint32)
+            np.bitwise_or.at(bcmask, y * words + (x >> 5), (np.uint32(1) << (x & 31).astype(np.uint32)))
+            self.desc = torch.from_numpy(desc.reshape(ny, nx)).to(device)
+            self.bcmask = torch.from_numpy(bcmask.reshape(ny, words)).to(device)
             g.desc = self.desc.data_ptr()
             g.bcmask = self.bcmask.data_ptr()
             # plain inlet / outlet columns: the batched boundary-free step applies
             # them itself, its boundary-node pass skips them
-            edge = np.zeros((nx, ny), dtype=bool)
-            g.edge_inlet_desc, g.edge_outlet_desc = self._edge_desc(src, desc, special, edge)
+            edge = np.zeros(nodes.size, dtype=bool)
+            g.edge_inlet_desc, g.edge_outlet_desc = self._edge_desc(nx, ny, nodes, src, packed, edge)
             # linear indices y*nx + x of the boundary nodes, for the boundary-node
             # pass: the other boundary nodes first, then the plain edge nodes
-            core = np.flatnonzero((special & ~edge).T.reshape(-1))
-            tail = np.flatnonzero(edge.T.reshape(-1))
-            nodes = np.concatenate([core, tail]).astype(np.int32)
-            self.bcnodes = torch.from_numpy(nodes).to(device)
+            order = np.concatenate([nodes[~edge], nodes[edge]]).astype(np.int32)
+            self.bcnodes = torch.from_numpy(order).to(device)
             g.bcnodes = self.bcnodes.data_ptr()
-            g.n_bcnodes = int(nodes.size)
-            g.n_bcnodes_edge = int(tail.size)
+            g.n_bcnodes = int(order.size)
+            g.n_bcnodes_edge = int(edge.sum())
             g.n_kset, g.n_cset = len(ktab), len(ctab)
-            for s in range(len(ktab)):
+            for s_ in range(len(ktab)):
                 for i in range(9):
-                    g.kconst[s][i] = float(ktab[s, i])
-            for s in range(len(ctab)):
+                    g.kconst[s_][i] = float(ktab[s_, i])
+            for s_ in range(len(ctab)):
                 for i in range(9):
-                    g.cconst[s][i] = float(ctab[s, i])
+                    g.cconst[s_][i] = float(ctab[s_, i])
         else:
             self.desc = self.bcmask = self.bcnodes = None
         if pressure is not None:
@@ -112,27 +123,29 @@ class CompiledGeometry:
         self.struct = g
 
     @staticmethod
-    def _edge_desc(src, desc, special, edge):
+    def _edge_desc(nx, ny, nodes, src, packed, edge):
         """(inlet, outlet) descriptors of the plain edge nodes, 0 for none; marks
-        those nodes in ``edge``.  Plain inlet: all nine sources CONST (the most
-        common such descriptor of column 0); plain outlet: directions 3, 6, 7
-        OUTLET and the others PULL (column nx-1).  A column qualifies only when
-        every node of it has a descriptor, so that a kernel may apply the form
-        to the whole column and leave the other nodes to the pass."""
-        nx = src.shape[0]
+        those nodes in ``edge`` (over the boundary nodes ``nodes``).  Plain inlet:
+        all nine sources CONST (the most common such descriptor of column 0);
+        plain outlet: directions 3, 6, 7 OUTLET and the others PULL (column
+        nx-1).  A column qualifies only when every node of it has a descriptor,
+        so that a kernel may apply the form to the whole column and leave the
+        other nodes to the pass."""
         out = []
-        for x, want in ((0, np.full(9, CONST)),
-                        (nx - 1, np.array([OUTLET if i in (3, 6, 7) else PULL for i in range(9)]))):
-            if nx < 2 or not special[x, :].all():
+        x = nodes % nx
+        for col, want in ((0, np.full(9, CONST)),
+                          (nx - 1, np.array([OUTLET if i in (3, 6, 7) else PULL for i in range(9)]))):
+            on = x == col
+            if nx < 2 or int(on.sum()) != ny:
                 out.append(0)
                 continue
-            plain = (src[x] == want.astype(np.uint32)).all(axis=-1)
+            plain = on & (src == want.astype(np.uint32)).all(axis=-1)
             if not plain.any():
                 out.append(0)
                 continue
-            vals, counts = np.unique(desc[x, plain], return_counts=True)
+            vals, counts = np.unique(packed[plain], return_counts=True)
             d = int(vals[np.argmax(counts)])
-            edge[x, :] |= plain & (desc[x, :] == d)
+            edge |= plain & (packed == d)
             out.append(d)
         return out[0], out[1]
 
