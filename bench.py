@@ -307,7 +307,7 @@ def bench_serve(P, n=60, rates=None):
     offered loads below its capacity (per-rate rows); error of f16 results
     against their solo fx64 solve on a sample."""
     import torch
-    rates = rates or {"f16": (8.0, 14.0), "fx64": (3.0,), "f64": (1.0,)}
+    rates = rates or {"f16": (8.0, 16.0), "fx64": (4.0,), "f64": (1.5,)}
     out = {}
     for storage, rs in rates.items():
         rows = []
@@ -337,8 +337,8 @@ def bench_serve_sweep(P, window_s=60.0, rates=None):
     """Offered load swept up to and beyond each storage's capacity, every rate
     with at least ``window_s`` seconds of arrivals (n = rate x window requests,
     a prefix of one seeded stream): solves/s, p50 and p99 latency per rate."""
-    rates = rates or {"f16": (4.0, 8.0, 12.0, 16.0, 20.0, 24.0), "fx64": (1.5, 3.0, 4.5, 6.0, 8.0),
-                      "f64": (0.5, 1.0, 1.5, 2.0)}
+    rates = rates or {"f16": (8.0, 16.0, 24.0, 32.0, 40.0), "fx64": (3.0, 6.0, 9.0, 12.0),
+                      "f64": (1.0, 2.0, 3.0)}
     out = {}
     for storage, rs in rates.items():
         out[storage] = []
