@@ -154,6 +154,20 @@ class ServingEngine:
         # while the GPU runs a tick; its copies and kernels go on this stream
         self.side = torch.cuda.Stream(device=self.batch.device)
 
+    def _next_admissions(self, waiting, extra=2):
+        """The head of the queue that the next admissions can take (free slots,
+        room in the HBM budget), plus ``extra`` more: the requests worth
+        preparing now, with their initial states held beyond the budget for a
+        few requests at most."""
+        out, used, slots = [], self.used, self.max_slots - len(self.live)
+        for r in waiting:
+            if slots <= 0 or used + self.state_bytes(r) > self.hbm_budget:
+                break
+            out.append(r)
+            used += self.state_bytes(r)
+            slots -= 1
+        return waiting[:len(out) + extra]
+
     def _prepare(self, reqs):
         """Compile the boundary descriptor and build the initial state on the
         device for requests about to be admitted, on the side stream."""
@@ -230,7 +244,7 @@ class ServingEngine:
             while i < len(pending) and (pending[i].arrival <= now or not realtime):
                 waiting.append(pending[i])
                 i += 1
-            self._prepare(waiting[:max(0, self.max_slots - len(self.live)) + 4])
+            self._prepare(self._next_admissions(waiting))
             finished = [(r, m) for r, m in self.live if b.done(m)]
             if finished:
                 for r, m in finished:

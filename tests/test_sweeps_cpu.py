@@ -50,3 +50,19 @@ def test_request_stream_is_the_same_at_every_rate():
             assert 64 <= nx <= 2048 and 16 <= ny <= 512 and 1e-4 <= params["drho"] <= 1e-2
         else:
             assert (nx, ny) == (420, 180)
+
+
+def test_next_admissions_respect_slots_and_budget():
+    """The requests the serving loop prepares while the GPU runs a tick: the
+    head of the queue that fits the free slots and the HBM budget, plus two."""
+    from types import SimpleNamespace
+    reqs = [SimpleNamespace(rid=k, size=100 * (k + 1)) for k in range(10)]
+    eng = SimpleNamespace(used=0, max_slots=4, live=[], hbm_budget=10 ** 9,
+                          state_bytes=lambda r: r.size)
+    take = serving.ServingEngine._next_admissions
+    assert [r.rid for r in take(eng, reqs)] == [0, 1, 2, 3, 4, 5]      # 4 slots + 2
+    eng.live = [None] * 4
+    assert [r.rid for r in take(eng, reqs)] == [0, 1]                  # no slot free
+    eng.live, eng.hbm_budget = [], 350
+    assert [r.rid for r in take(eng, reqs)] == [0, 1, 2, 3]            # 100 + 200 fit, then 2 more
+    assert take(eng, []) == []
