@@ -83,7 +83,6 @@ class Batch:
         self._default_shape(0)
         self.blocks = ONE_TILE_PER_BLOCK if blocks is None else blocks
         self.rows = int(rows)           # runs per tile (0: chosen from the batch size)
-        self.tail_small = True          # one-run tiles for the lattices of the last wave (_tail_rows)
         self.bc_chunks = -1             # boundary-node plan of the work table (-1: sources in the step)
         self.gbase = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.g = 0                    # host mirror of the global step
@@ -171,30 +170,10 @@ class Batch:
             return 1
         return 8 if self.storage in ("f16", "bf16") else 4
 
-    def _tail_rows(self, rows: int) -> list:
-        """Runs per tile of each member.  Tiles run in table order, so the
-        lattices at the end of the table make the last wave of blocks; with
-        ``rows`` > 1 those covering the last wave's worth of nodes (every SM
-        holding 2048 threads of ``npt``-node chunks, ``rows`` runs each) take
-        one run per tile, so that the last wave ends in small tiles and the GPU
-        does not idle behind a few large ones.  Tile shapes do not change results."""
-        out = [rows] * len(self.members)
-        if rows <= 1 or self.tail_small is False:
-            return out
-        sms = torch.cuda.get_device_properties(self.device).multi_processor_count
-        tail, acc = sms * 2048 * self.npt * rows, 0
-        for j in range(len(self.members) - 1, -1, -1):
-            if acc >= tail:
-                break
-            out[j] = 1
-            acc += self.members[j].nodes
-        return out
-
     def _build(self, with_probes=True):
         n = len(self.members)
         self._default_shape(self.nodes)
         rows = self._rows()
-        member_rows = self._tail_rows(rows)
         arr = (BatchLatticeC * n)()
         self._keep = []
         for j, m in enumerate(self.members):
@@ -213,7 +192,7 @@ class Batch:
             c.seed = int(m.seed) & 0xFFFFFFFF
             c.flags = (_lib.FLAG_STOCHASTIC if self.stochastic else 0) | \
                 {True: _lib.FLAG_BC_INLINE, False: _lib.FLAG_BC_SPLIT}.get(self.inline_bc, 0)
-            c.rows = member_rows[j]
+            c.rows = rows
         size = int(_lib.load().lbm_batch_table_bytes(n))
         self.table = torch.empty(size, dtype=torch.uint8, device=self.device)
         tiles, chunks = ctypes.c_int32(0), ctypes.c_int32(0)
