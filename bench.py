@@ -28,7 +28,8 @@ sys.path.insert(0, ROOT)
 
 BYTES_PER_NODE = {"fx64": 144, "f64": 144, "f32": 72, "f16": 36, "bf16": 36}
 # arithmetic of each storage's collision
-DTYPES = {"fx64": "int64+f32x2", "f64": "f64", "f32": "f32", "f16": "f32 (f16 storage)", "bf16": "f32 (bf16 storage)"}
+DTYPES = {"fx64": "int64+f32x2", "f64": "f64", "f32": "f32", "f16": "f32 (f16 storage)", "bf16": "f32 (bf16 storage)",
+          "f16r": "f32 (f16 storage, shifted)", "bf16r": "f32 (bf16 storage, shifted)"}
 
 
 def parse():
@@ -45,7 +46,7 @@ def parse():
                         "(inline), or chosen by the lattice size (auto)")
     p.add_argument("--no-extras", action="store_true", help="skip variants, e2e, CPU baseline and the other configs")
     p.add_argument("--workload", default="cavity",
-                   choices=["cavity", "shear", "vk", "batch", "serve", "serve_sweep", "batch_step"],
+                   choices=["cavity", "shear", "vk", "vk_seeds", "batch", "serve", "serve_sweep", "batch_step"],
                    help="cavity: the headline line; the others print one config's results and exit")
     p.add_argument("--configs", default="shear,vk,batch,serve", help="other configs added to the headline line")
     return p.parse_args()
@@ -142,11 +143,55 @@ def phase_lag(ref, other, period_guess, window):
     return lag
 
 
+def bench_vk_seeds(P, steps=100000, seeds=8):
+    """Spread of the 16-bit storages' errors over stochastic-rounding seeds on
+    the von Karman precision study (420x180, Re 100): ``seeds`` members with
+    seeds 1000.. in one batch per storage (f16, f16r, bf16, bf16r; the shifted
+    ones with the inlet velocity (0.1, 0) as the reference) against one fx64
+    run: velocity L2 at 2000, 5000 and 10000 steps and the Strouhal error of
+    u_y at (300, 90) over ``steps`` steps (sub-bin estimate), each as
+    (mean, min, max)."""
+    import torch
+    from lattice_boltzmann_parallel_solver_gb300.batch import Batch, Member
+    f, rho, u, omega, bnd = P.scenarios.von_karman(420, 180, plate=40, re=100, seed=0)
+    cps = (2000, 5000, 10000)
+
+    def run(storage, n):
+        ms = [Member(420, 180, omega, bnd, steps=steps, probe=(300, 90), f0=f, rho0=rho, u0=u, seed=1000 + k,
+                     dev_ref=(0.1, 0.0) if storage in ("f16r", "bf16r") else None) for k in range(n)]
+        b = Batch(ms, storage=storage).start()
+        us = {}
+        for c in cps:
+            b.run_graph(c - 1 - b.g, chunk=1000)
+            us[c] = [b.read(j, want_f=False)[2] for j in range(n)]
+        b.run_graph(chunk=1000)
+        sts = []
+        for j in range(n):
+            uy = b.probe_trace(j)[:, 1]
+            sts.append(P.analysis.spectral_peak(uy, start=uy.numel() // 2)[0])
+        return us, sts
+
+    def spread(v):
+        return [float(np.mean(v)), float(np.min(v)), float(np.max(v))]
+
+    ref_us, ref_st = run("fx64", 1)
+    out = {"seeds": seeds, "steps": steps}
+    for st in ("f16", "f16r", "bf16", "bf16r"):
+        us, sts = run(st, seeds)
+        r = {"velocity_l2_rel_err_%d" % c: spread([float(torch.linalg.norm(x - ref_us[c][0]) /
+                                                        torch.linalg.norm(ref_us[c][0])) for x in us[c]])
+             for c in cps}
+        r["strouhal_rel_err"] = spread([abs(x - ref_st[0]) / ref_st[0] for x in sts])
+        out[st] = r
+    return out
+
+
 def bench_vk(P, steps=100000):
     """Von Karman precision study: 420x180, plate 40 at x=105 offset +1, inlet
     (0.1, 0) with seeded U(-1e-3, 1e-3) u_y, the reference's outlet,
     top/bottom bounce-back, Re 100; float64 storage against fx64 / float32 / f16 / bf16
-    storage: velocity L2 error at fixed steps (before and after the onset of
+    storage and the reference-shifted f16r / bf16r (reference velocity the
+    inlet's (0.1, 0)): velocity L2 error at fixed steps (before and after the onset of
     shedding), the Strouhal number of u_y at (300, 90) by a sub-bin estimate
     with its resolution, and the error split into phase (the lag of the
     shedding cycle) and the rest (the L2 error against the float64 field at
@@ -159,7 +204,8 @@ def bench_vk(P, steps=100000):
     out, ref_u, traces = {}, {}, {}
 
     def run(storage, upto, cps):
-        m = Member(lx, ly, omega, bnd, steps=upto, probe=(300, 90), f0=f, rho0=rho, u0=u)
+        m = Member(lx, ly, omega, bnd, steps=upto, probe=(300, 90), f0=f, rho0=rho, u0=u,
+                   dev_ref=(0.1, 0.0) if storage in ("f16r", "bf16r") else None)
         b = Batch([m], storage=storage).start()
         us, ms_total, done = {}, 0.0, 1
         for c in cps:
@@ -168,7 +214,7 @@ def bench_vk(P, steps=100000):
             us[c] = b.read(0, want_f=False)[2]
         return b, us, ms_total
 
-    for storage in ("f64", "fx64", "f32", "f16", "bf16"):
+    for storage in ("f64", "fx64", "f32", "f16", "bf16", "f16r", "bf16r"):
         b, us, ms_total = run(storage, steps, checkpoints)
         uy = b.probe_trace(0)[:, 1].cpu().numpy()
         traces[storage] = uy
@@ -528,8 +574,8 @@ def main():
 
     torch.cuda.set_device(local)
     if args.workload != "cavity":
-        fn = {"shear": bench_shear, "vk": bench_vk, "batch": bench_batch, "serve": bench_serve,
-              "serve_sweep": bench_serve_sweep, "batch_step": batch_step}[args.workload]
+        fn = {"shear": bench_shear, "vk": bench_vk, "vk_seeds": bench_vk_seeds, "batch": bench_batch,
+              "serve": bench_serve, "serve_sweep": bench_serve_sweep, "batch_step": batch_step}[args.workload]
         print(json.dumps(fn(P)), flush=True)
         return
     if world > 1:

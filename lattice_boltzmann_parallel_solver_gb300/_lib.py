@@ -21,7 +21,7 @@ SRC_PULL, SRC_BOUNCE, SRC_CONST, SRC_OUTLET = 0, 1, 2, 3
 KSET_SHIFT, CSET_SHIFT = 18, 22
 MAX_SETS = 16
 
-STORE_F64, STORE_F32, STORE_F16S, STORE_BF16S, STORE_FX64 = 0, 1, 2, 3, 4
+STORE_F64, STORE_F32, STORE_F16S, STORE_BF16S, STORE_FX64, STORE_F16R, STORE_BF16R = 0, 1, 2, 3, 4, 5, 6
 FLAG_EXACT = 1
 FLAG_GENERIC = 2
 FLAG_NPT_SHIFT = 4
@@ -48,6 +48,7 @@ class Geometry(C.Structure):
         ("outlet", i32),
         ("bcnodes", vp), ("n_bcnodes", i32),
         ("edge_inlet_desc", C.c_uint32), ("edge_outlet_desc", C.c_uint32), ("n_bcnodes_edge", i32),
+        ("dev_ref_ux", f64), ("dev_ref_uy", f64),
     ]
 
 

@@ -18,7 +18,7 @@ import torch
 from . import _arrays as A
 from . import _lib
 from .geometry import empty_geometry
-from .lattice import STORAGES
+from .lattice import REF_SHIFTED, SIXTEEN_BIT, STORAGES, with_dev_ref
 
 
 BatchLatticeC = _lib.BatchLattice
@@ -37,6 +37,7 @@ class Member:
     rho0: object = None
     u0: object = None
     seed: int = 0                # random bits of the stochastic rounding (16-bit storages)
+    dev_ref: tuple = None        # reference velocity of the "f16r" / "bf16r" storages (default (0, 0))
     # filled in by the batch
     geo: object = None
     pitch: int = 0
@@ -69,9 +70,10 @@ class Batch:
         keep every SM busy, 1 otherwise).  ``blocks``: the default (None) is a
         plain grid of one tile per block, 0 persistent blocks filling the GPU
         that walk contiguous spans of tiles, any other number that many
-        persistent blocks."""
+        persistent blocks.  The reference-shifted storages ("f16r", "bf16r",
+        each member's ``dev_ref``) run at 4 x 128 only."""
         A.require_cuda()
-        self.stochastic = storage in ("f16", "bf16") if stochastic is None else bool(stochastic)
+        self.stochastic = storage in SIXTEEN_BIT if stochastic is None else bool(stochastic)
         self.storage = storage
         self.store_id, self.pop_dtype, self.aux_dtype = STORAGES[storage]
         self.device = torch.device(device)
@@ -97,6 +99,7 @@ class Batch:
 
     def _alloc(self, m: Member):
         m.geo = m.boundary.geometry(m.nx, m.ny) if m.boundary is not None else empty_geometry(m.nx, m.ny)
+        m.geo = with_dev_ref(m.geo, self.storage, m.dev_ref)
         if not m.geo.fusable:
             raise NotImplementedError("the outlet must sit on column nx-1")
         m.pitch = (m.nx + 31) // 32 * 32
@@ -149,8 +152,8 @@ class Batch:
         """Default nodes per thread / threads per tile: below 2^20 nodes (one
         launch per step, boundary sources inside, row-segment tiles) 2 x 128
         for the 16-bit storages and 1 x 128 for fx64; above (boundary-free step
-        over runs across row ends, then the boundary-node pass) 4 x 64 and
-        1 x 64."""
+        over runs across row ends, then the boundary-node pass) 4 x 128 and
+        1 x 64; 4 x 128 always for the reference-shifted storages."""
         split = self.inline_bc is False or (self.inline_bc is None and nodes >= (1 << 20))
         if self._auto_shape[0]:
             self.npt = {"fx64": 1, "f64": 2, "f16": 4 if split else 2, "bf16": 4 if split else 2}.get(self.storage, 4)
@@ -168,7 +171,7 @@ class Batch:
         sms = torch.cuda.get_device_properties(self.device).multi_processor_count
         if runs < 64 * sms:
             return 1
-        return 8 if self.storage in ("f16", "bf16") else 4
+        return 8 if self.storage in SIXTEEN_BIT else 4
 
     def _build(self, with_probes=True):
         n = len(self.members)
@@ -290,8 +293,10 @@ def autotune(batch: Batch, candidates=None, steps: int = 6, warmup: int = 2):
     (probes off) and the global step counter is reset afterwards."""
     sms = torch.cuda.get_device_properties(batch.device).multi_processor_count
     if candidates is None:
-        npts = {"fx64": (1, 2), "f16": (2, 4, 8), "bf16": (2, 4, 8)}.get(batch.storage, (2, 4))
-        candidates = [(p, t, b, r) for p in npts for t in (64, 128, 256) for b in (0, 8 * sms, ONE_TILE_PER_BLOCK)
+        npts = {"fx64": (1, 2), "f16": (2, 4, 8), "bf16": (2, 4, 8), "f16r": (4,), "bf16r": (4,)}.get(
+            batch.storage, (2, 4))
+        threads = (128,) if batch.storage in REF_SHIFTED else (64, 128, 256)
+        candidates = [(p, t, b, r) for p in npts for t in threads for b in (0, 8 * sms, ONE_TILE_PER_BLOCK)
                       for r in (1, 2, 4, 8, 16)]
     best, results = None, []
     for cand in candidates:

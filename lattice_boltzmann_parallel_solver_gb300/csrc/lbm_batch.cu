@@ -48,6 +48,7 @@ int lbm_batch_build(const lbm_batch_lattice* lat, int32_t n, int32_t npt, int32_
     e.P.probe_count = L.probe_count;
     e.P.seed = L.seed;
     e.P.qc = fx::q_consts(L.omega);
+    set_shift(e.P);
     e.P.sr = (L.flags & LBM_FLAG_STOCHASTIC) != 0;
     if (L.probe_buf != nullptr && L.probe_count == nullptr)
       return set_error(LBM_ERR_ARG, "a probe needs its counter");

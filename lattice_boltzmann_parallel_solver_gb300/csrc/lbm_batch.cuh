@@ -63,8 +63,9 @@ __device__ __forceinline__ int owner_of(const int* __restrict__ start, int n, in
   return lo;
 }
 
-// One tile of lattice `e` (staged in shared memory) at global step g.
-template <int STORE, int NPT, int THREADS, bool HAS_BC>
+// One tile of lattice `e` (staged in shared memory) at global step g; SHIFT:
+// the reference-shifted 16-bit storages.
+template <int STORE, int NPT, int THREADS, bool HAS_BC, bool SHIFT>
 __device__ __forceinline__ void batch_tile(const BatchEntry& e, int local, int g) {
   const bool odd = (g - e.s0) & 1;
   const void* pin = odd ? e.pop_b : e.pop_a;
@@ -83,8 +84,8 @@ __device__ __forceinline__ void batch_tile(const BatchEntry& e, int local, int g
       if (pressure) fused_fx_body<NPT, HAS_BC, HAS_BC, !HAS_BC>(e.P, pin, pout, ain, aout, x0, y);
       else fused_fx_body<NPT, HAS_BC, false, !HAS_BC>(e.P, pin, pout, ain, aout, x0, y);
     } else {
-      if (pressure) fused_v2_body<STORE, NPT, HAS_BC, HAS_BC, !HAS_BC>(e.P, pin, pout, ain, aout, x0, y, seed);
-      else fused_v2_body<STORE, NPT, HAS_BC, false, !HAS_BC>(e.P, pin, pout, ain, aout, x0, y, seed);
+      if (pressure) fused_v2_body<STORE, NPT, HAS_BC, HAS_BC, !HAS_BC, SHIFT>(e.P, pin, pout, ain, aout, x0, y, seed);
+      else fused_v2_body<STORE, NPT, HAS_BC, false, !HAS_BC, SHIFT>(e.P, pin, pout, ain, aout, x0, y, seed);
     }
   };
   if constexpr (HAS_BC) {
@@ -125,7 +126,7 @@ __device__ __forceinline__ void batch_tile(const BatchEntry& e, int local, int g
 // belong to one lattice: the owner search and the entry staging happen once per
 // lattice the span touches, not once per tile, and the spans differ by at most
 // one tile (no tail of partly filled waves).
-template <int STORE, int NPT, int THREADS, bool HAS_BC>
+template <int STORE, int NPT, int THREADS, bool HAS_BC, bool SHIFT>
 __global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS, HAS_BC>())
     batch_kernel(const BatchEntry* __restrict__ tab, const int* __restrict__ tile_start, int n_inst,
                  int total_tiles, const int* __restrict__ gbase, int k) {
@@ -152,7 +153,7 @@ __global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS,
       } while (tile >= next);
       stage_entry<THREADS, HAS_BC>(tab, lo, ebuf);
     }
-    if (g >= e.s0 && g < e.s_end) batch_tile<STORE, NPT, THREADS, HAS_BC>(e, tile - first, g);
+    if (g >= e.s0 && g < e.s_end) batch_tile<STORE, NPT, THREADS, HAS_BC, SHIFT>(e, tile - first, g);
   }
 }
 
@@ -179,7 +180,7 @@ __device__ __forceinline__ int owner_of_staged(const int* __restrict__ start, in
   return a;
 }
 
-template <int STORE, int NPT, int THREADS, bool HAS_BC>
+template <int STORE, int NPT, int THREADS, bool HAS_BC, bool SHIFT>
 __global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS, HAS_BC>())
     batch_grid_kernel(const BatchEntry* __restrict__ tab, const int* __restrict__ tile_start, int n_inst,
                       const int* __restrict__ gbase, int k) {
@@ -190,7 +191,7 @@ __global__ void __launch_bounds__(THREADS, batch_min_blocks<STORE, NPT, THREADS,
   stage_entry<THREADS, HAS_BC>(tab, lo, ebuf);
   const int g = *gbase + k;
   if (g < e.s0 || g >= e.s_end) return;
-  batch_tile<STORE, NPT, THREADS, HAS_BC>(e, tile - __ldg(tile_start + lo), g);
+  batch_tile<STORE, NPT, THREADS, HAS_BC, SHIFT>(e, tile - __ldg(tile_start + lo), g);
 }
 
 // The batched boundary-node pass: after batch_kernel<..., false> stepped every
@@ -213,7 +214,7 @@ inline int64_t pass_nodes(const GeoK& g) {
   return (g.bcmask != nullptr ? (int64_t)(g.n_bcnodes - g.n_bcnodes_edge) : 0) + (g.pressure ? 2 * (int64_t)g.ny : 0);
 }
 
-template <int STORE>
+template <int STORE, bool SHIFT>
 __global__ void __launch_bounds__(kFixupChunk)
     batch_fixup_kernel(const BatchEntry* __restrict__ tab, const int* __restrict__ bc_start, int n_inst,
                        const int* __restrict__ gbase, int k) {
@@ -252,15 +253,15 @@ __global__ void __launch_bounds__(kFixupChunk)
     else fused_fx_body<1, true, false>(e.P, pin, pout, ain, aout, x, y);
   } else {
     const uint32_t seed = hash32(e.P.seed + (uint32_t)(g - e.s0));
-    if (e.P.g.pressure) fused_v2_body<STORE, 1, true, true>(e.P, pin, pout, ain, aout, x, y, seed);
-    else fused_v2_body<STORE, 1, true, false>(e.P, pin, pout, ain, aout, x, y, seed);
+    if (e.P.g.pressure) fused_v2_body<STORE, 1, true, true, false, SHIFT>(e.P, pin, pout, ain, aout, x, y, seed);
+    else fused_v2_body<STORE, 1, true, false, false, SHIFT>(e.P, pin, pout, ain, aout, x, y, seed);
   }
 }
 
 // one copy per translation unit (each unit launches its own)
 static __global__ void batch_advance_kernel(int* gbase, int k) { *gbase += k; }
 
-template <int STORE, int NPT, int THREADS, bool HAS_BC>
+template <int STORE, int NPT, int THREADS, bool HAS_BC, bool SHIFT = false>
 inline int launch_batch(const void* table, int n, int tiles, int bc_chunks, int* gbase, int nsteps, int blocks,
                         cudaStream_t s) {
   const BatchEntry* tab = static_cast<const BatchEntry*>(table);
@@ -274,7 +275,8 @@ inline int launch_batch(const void* table, int n, int tiles, int bc_chunks, int*
       int per_sm = 0, sms = 0, dev = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<STORE, NPT, THREADS, HAS_BC>, THREADS, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel<STORE, NPT, THREADS, HAS_BC, SHIFT>,
+                                                    THREADS, 0);
       fill = std::max(1, sms * std::max(1, per_sm));
     }
     blocks = fill;
@@ -285,16 +287,16 @@ inline int launch_batch(const void* table, int n, int tiles, int bc_chunks, int*
   blocks = std::min(blocks, std::max(1, tiles));
   for (int k = 0; k < nsteps; ++k) {
     if (plain && tiles > 0) {
-      batch_grid_kernel<STORE, NPT, THREADS, HAS_BC><<<tiles, THREADS, 0, s>>>(tab, start, n, gbase, k);
+      batch_grid_kernel<STORE, NPT, THREADS, HAS_BC, SHIFT><<<tiles, THREADS, 0, s>>>(tab, start, n, gbase, k);
       count_launch();
       if (int e = check_launch("batch_grid_kernel")) return e;
     } else {
-      batch_kernel<STORE, NPT, THREADS, HAS_BC><<<blocks, THREADS, 0, s>>>(tab, start, n, tiles, gbase, k);
+      batch_kernel<STORE, NPT, THREADS, HAS_BC, SHIFT><<<blocks, THREADS, 0, s>>>(tab, start, n, tiles, gbase, k);
       count_launch();
       if (int e = check_launch("batch_kernel")) return e;
     }
     if (!HAS_BC && bc_chunks > 0) {
-      batch_fixup_kernel<STORE><<<bc_chunks, kFixupChunk, 0, s>>>(tab, bc_start, n, gbase, k);
+      batch_fixup_kernel<STORE, SHIFT><<<bc_chunks, kFixupChunk, 0, s>>>(tab, bc_start, n, gbase, k);
       count_launch();
       if (int e = check_launch("batch_fixup_kernel")) return e;
     }
@@ -325,6 +327,12 @@ int batch_launch_split(const void* table, int n, int tiles, int bc_chunks, int s
     LBM_BATCH_NPT(LBM_STORE_BF16S, 2, HAS_BC)                                                                \
     LBM_BATCH_NPT(LBM_STORE_BF16S, 4, HAS_BC)                                                                \
     LBM_BATCH_NPT(LBM_STORE_BF16S, 8, HAS_BC)                                                                \
+    if (storage == LBM_STORE_F16R && npt == 4 && threads == 128)                                             \
+      return launch_batch<LBM_STORE_F16S, 4, 128, HAS_BC, true>(table, n, tiles, bc_chunks, gbase, nsteps,   \
+                                                                blocks, s);                                  \
+    if (storage == LBM_STORE_BF16R && npt == 4 && threads == 128)                                            \
+      return launch_batch<LBM_STORE_BF16S, 4, 128, HAS_BC, true>(table, n, tiles, bc_chunks, gbase, nsteps,  \
+                                                                 blocks, s);                                 \
     return set_error(LBM_ERR_UNSUPPORTED, "no batched kernel for this storage / npt / threads");              \
   } while (0)
 #define LBM_BATCH_CASE(ST, NP, TH, HAS_BC)               \

@@ -381,6 +381,48 @@ __device__ __forceinline__ void collide_dev2(float2 d[9], float2 drho, float2 rh
 #undef LBM_DPAIR2
 }
 
+// Constants of the reference-shifted 16-bit storages in the working units
+// (scale s): stored numbers D_i = d_i - sig_i, sig_i = s (c_i - w_i) with c_i
+// the equilibrium at the reference velocity.  The collision works on D
+// directly: D_i' = (1 - omega) D_i + omega (E_i - sig_i), E the deviation
+// equilibrium of the moments of d = D + sig.  -omega sig_i is split per
+// direction pair (1,3), (2,4), (5,7), (6,8) into an even part qe and an odd
+// part qo (-omega sig of the first direction = qe + qo, of the second
+// qe - qo), q0 for direction 0; sig holds the values these constants imply,
+// S = sum_i sig_i, oS = omega S, (sx, sy) = sum_i c_i sig_i.
+struct ShiftK {
+  float sig[9];
+  float q0, qe[4], qo[4];
+  float S, oS, sx, sy;
+};
+
+// collide_dev2 on stored numbers of a reference-shifted storage: sum, jx, jy
+// are the moments of D with (sx, sy) already added to jx, jy; the mass
+// offset S enters through oS
+__device__ __forceinline__ void collide_dev2_ref(float2 d[9], float2 drho, float2 rho, float2 ux, float2 uy,
+                                                 float omega, const ShiftK& h) {
+  const float2 om1 = f2c(1.0f - omega), om = f2c(omega);
+  const float2 Bd = mul2(f2c(-1.5f), fma2(ux, ux, mul2(uy, uy)));
+  const float2 orho = mul2(om, rho), odr = fma2(om, drho, f2c(h.oS));
+  const float2 W0 = mul2(orho, f2c(wf(0))), W1 = mul2(orho, f2c(wf(1))), W5 = mul2(orho, f2c(wf(5)));
+  const float2 V1 = mul2(f2c(3.0f), W1), V5 = mul2(f2c(3.0f), W5);
+  d[0] = fma2(om1, d[0], fma2(W0, Bd, fma2(odr, f2c(wf(0)), f2c(h.q0))));
+  const float2 d58 = add2(ux, uy), d67 = sub2(uy, ux);
+#define LBM_RPAIR2(I, J, V, W, WI, VV, P)                             \
+  {                                                                   \
+    const float2 t = fma2(mul2(f2c(4.5f), (V)), (V), Bd);             \
+    const float2 s = fma2((W), t, fma2(odr, f2c(wf(WI)), f2c(h.qe[P]))); \
+    const float2 m = fma2((VV), (V), f2c(h.qo[P]));                   \
+    d[I] = fma2(om1, d[I], add2(s, m));                               \
+    d[J] = fma2(om1, d[J], sub2(s, m));                               \
+  }
+  LBM_RPAIR2(1, 3, ux, W1, 1, V1, 0)
+  LBM_RPAIR2(2, 4, uy, W1, 1, V1, 1)
+  LBM_RPAIR2(5, 7, d58, W5, 5, V5, 2)
+  LBM_RPAIR2(6, 8, d67, W5, 5, V5, 3)
+#undef LBM_RPAIR2
+}
+
 // equilibrium with FMAs (used where the fast path needs feq itself)
 template <typename R>
 __device__ __forceinline__ void bracket9_fast(R ux, R uy, R br[9]) {

@@ -29,6 +29,8 @@ struct GeoK {
   uint32_t edge_in_desc, edge_out_desc;
   int n_bcnodes_edge;
   double edge_in_f[9];
+  // reference velocity of the reference-shifted 16-bit storages
+  double dev_ref_ux, dev_ref_uy;
 };
 
 struct View {
@@ -66,6 +68,12 @@ struct KParams {
   // hash32(seed + *step_dev) (seed then holds the unhashed base + step index),
   // so a captured CUDA graph of steps draws new bits on every replay
   const int32_t* step_dev;
+  // the reference-shifted 16-bit storages (LBM_STORE_F16R, LBM_STORE_BF16R):
+  // their constants in the working units of f16 ([0], scale 1024) and bf16
+  // ([1], scale 1: sig in populations), filled by set_shift from g.dev_ref_*
+  // and omega; dev_shift selects them in the generic kernel
+  ShiftK shf[2];
+  int dev_shift;
   // fixed-point storage: constants of its collision
   fx::QConsts qc;
 };
@@ -113,7 +121,7 @@ __device__ __forceinline__ void write_probe(const KParams& P, int x, int y, R ux
 // 32-bit element indices (9 * plane < 2^31).  Boundary descriptors and the
 // pressure rewrite are compiled in only where a geometry may have them.
 // ---------------------------------------------------------------------------
-template <int STORE, int NPT, bool HAS_BC, bool HAS_PRESSURE, bool EDGES = false>
+template <int STORE, int NPT, bool HAS_BC, bool HAS_PRESSURE, bool EDGES = false, bool SHIFT = false>
 __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_in_v, void* pop_out_v,
                                               const void* aux_in_v, void* aux_out_v, int x0, int y,
                                               uint32_t seed) {
@@ -123,6 +131,7 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
   // working values: scaled deviations s (f - w) for the shifted 16-bit storages
   // (the stored numbers themselves), f otherwise
   constexpr bool SH = St::kShifted;
+  static_assert(!SHIFT || SH, "the reference shift applies to the 16-bit deviations");
   constexpr R kS = [] {
     if constexpr (SH) return (R)St::kDev;
     else return R(1);
@@ -149,8 +158,22 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     if constexpr (SH) return St::dev(t);
     else return St::to_r(t, i);
   };
-  auto work_of_f = [&](R fv, int i) -> R { return SH ? (fv - wr<R>(i)) * kS : fv; };
-  auto f_of_work = [&](R v, int i) -> R { return SH ? fma(v, R(1) / kS, wr<R>(i)) : v; };
+  // SHIFT (LBM_STORE_F16R, LBM_STORE_BF16R): the working values are the
+  // stored numbers s (f_i - c_i) = s (f_i - w_i) - sig_i, c_i the equilibrium
+  // at the reference velocity (ShiftK)
+  const ShiftK& shk = P.shf[STORE == LBM_STORE_F16S ? 0 : 1];
+  auto sig = [&](int i) -> R {
+    if constexpr (SHIFT) return shk.sig[i];
+    else return R(0);
+  };
+  auto work_of_f = [&](R fv, int i) -> R {
+    if constexpr (SHIFT) return fma(fv - wr<R>(i), kS, -sig(i));
+    else return SH ? (fv - wr<R>(i)) * kS : fv;
+  };
+  auto f_of_work = [&](R v, int i) -> R {
+    if constexpr (SHIFT) return fma(v + sig(i), R(1) / kS, wr<R>(i));
+    else return SH ? fma(v, R(1) / kS, wr<R>(i)) : v;
+  };
 
   // the boundary mask word first: its latency overlaps the population loads
   const bool has_bc = HAS_BC && P.g.bcmask != nullptr;
@@ -230,9 +253,11 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
           const uint32_t s = (d >> (2 * i)) & 3u;
-          if (s == LBM_SRC_BOUNCE)
-            f[i][k] = ld_work(pin + opp(i) * plane + r0 + x, opp(i)) - (R)P.g.kconst[ks][i] * kS;
-          else if (s == LBM_SRC_CONST)
+          if (s == LBM_SRC_BOUNCE) {
+            R v = ld_work(pin + opp(i) * plane + r0 + x, opp(i)) - (R)P.g.kconst[ks][i] * kS;
+            if constexpr (SHIFT) v += sig(opp(i)) - sig(i);
+            f[i][k] = v;
+          } else if (s == LBM_SRC_CONST)
             f[i][k] = work_of_f((R)P.g.cconst[cs][i], i);
           else if (s == LBM_SRC_OUTLET && outlet_slot(i) >= 0 && aux_in != nullptr)
             f[i][k] = work_of_f(aux_in[outlet_slot(i) * ny + y], i);
@@ -297,10 +322,19 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
       for (int i = 0; i < 9; ++i) g2[i] = make_float2(f[i][k], f[i][k1]);
       float2 sum, jx, jy;
       moments9x2(g2, sum, jx, jy);
+      if constexpr (SHIFT) {
+        // the momentum of sig (its mass enters the collision through oS)
+        jx = add2(jx, f2c(shk.sx));
+        jy = add2(jy, f2c(shk.sy));
+      }
       const float2 rho = add2(f2c(kS), sum);  // s rho
       const float2 inv = make_float2(rho.x != 0.0f ? rcp_nr(rho.x) : 0.0f, rho.y != 0.0f ? rcp_nr(rho.y) : 0.0f);
       const float2 ux = mul2(jx, inv), uy = mul2(jy, inv);
-      collide_dev2(g2, sum, rho, ux, uy, omega);
+      if constexpr (SHIFT)
+        collide_dev2_ref(g2, sum, rho, ux, uy, omega, shk);
+      else
+        collide_dev2(g2, sum, rho, ux, uy, omega);
+      if constexpr (SHIFT) sum = add2(sum, f2c(shk.S));  // s (rho - 1) for the moments written out
       R ga[9], gb[9];
 #pragma unroll
       for (int i = 0; i < 9; ++i) {
@@ -658,7 +692,55 @@ inline bool to_geok(const lbm_geometry* g, GeoK& k) {
     if (k.edge_in_desc != 0u)
       for (int i = 0; i < 9; ++i) k.edge_in_f[i] = g->cconst[cs][i];
   }
+  const double ux = g->dev_ref_ux, uy = g->dev_ref_uy;
+  if (!(std::fabs(ux) < 0.5 && std::fabs(uy) < 0.5))
+    return set_error(LBM_ERR_ARG, "the deviation reference velocity must lie inside (-0.5, 0.5)"), false;
+  k.dev_ref_ux = ux;
+  k.dev_ref_uy = uy;
   return true;
+}
+
+// The constants of the reference-shifted storages (ShiftK) for P.g's reference
+// velocity and P.omega (1 where no collision runs).  The collision constants
+// are rounded first; sig, S and the momentum (sx, sy) are then derived from
+// the rounded values, so that the collision conserves mass exactly and the
+// boundary sources and the collision agree on the stored numbers.
+inline void set_shift(KParams& P) {
+  const double ux = P.g.dev_ref_ux, uy = P.g.dev_ref_uy;
+  const double om = (double)(float)(P.omega > 0.0 ? P.omega : 1.0);
+  static const int first[4] = {1, 2, 5, 6}, second[4] = {3, 4, 7, 8};
+  for (int v = 0; v < 2; ++v) {
+    const double scale = v == 0 ? 1024.0 : 1.0;
+    double sig[9];
+    for (int i = 0; i < 9; ++i) {
+      // s (c_i - w_i) = s w_i (3 c.u + 4.5 (c.u)^2 - 1.5 |u|^2) at rho = 1
+      const double cu = cx(i) * ux + cy(i) * uy;
+      sig[i] = scale * wd(i) * (3.0 * cu + 4.5 * cu * cu - 1.5 * (ux * ux + uy * uy));
+    }
+    ShiftK& h = P.shf[v];
+    h.q0 = (float)(-om * sig[0]);
+    double eff[9];
+    eff[0] = -(double)h.q0 / om;
+    for (int p = 0; p < 4; ++p) {
+      const int a = first[p], b = second[p];
+      h.qe[p] = (float)(-om * 0.5 * (sig[a] + sig[b]));
+      h.qo[p] = (float)(-om * 0.5 * (sig[a] - sig[b]));
+      eff[a] = -((double)h.qe[p] + (double)h.qo[p]) / om;
+      eff[b] = -((double)h.qe[p] - (double)h.qo[p]) / om;
+    }
+    double S = 0.0, mx = 0.0, my = 0.0, oS = -(double)h.q0;
+    for (int i = 0; i < 9; ++i) {
+      h.sig[i] = (float)eff[i];
+      S += eff[i];
+      mx += cx(i) * eff[i];
+      my += cy(i) * eff[i];
+    }
+    for (int p = 0; p < 4; ++p) oS -= 2.0 * (double)h.qe[p];
+    h.S = (float)S;
+    h.oS = (float)oS;
+    h.sx = (float)mx;
+    h.sy = (float)my;
+  }
 }
 
 inline int check_omega(double omega) {

@@ -34,6 +34,18 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
   const int64_t r0 = (int64_t)y * P.pitch;
   using A = typename St::A;
   const A* aux_in = static_cast<const A*>(P.aux_in);
+  // reference-shifted 16-bit storages: the stored deviation is taken from
+  // c_i = w_i + sig_i instead of w_i
+  const bool shift = St::kShifted && P.dev_shift;
+  auto ld = [&](const T* p, int i) -> R {
+    const R v = St::ld(p, i);
+    if constexpr (St::kShifted) return shift ? v + (R)P.shf[1].sig[i] : v;
+    else return v;
+  };
+  auto st = [&](T* p, R v, int i) {
+    if constexpr (St::kShifted) St::st(p, shift ? v - (R)P.shf[1].sig[i] : v, i);
+    else St::st(p, v, i);
+  };
 
   R f[9];
   if (MODE == MODE_INIT) {
@@ -50,7 +62,7 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
     for (int i = 0; i < 9; ++i) {
       const int xs = cx(i) == 1 ? xm : (cx(i) == -1 ? xp : x);
       const int64_t rs = cy(i) == 1 ? rm : (cy(i) == -1 ? rp : r0);
-      f[i] = St::ld(pin + i * P.plane + rs + xs, i);
+      f[i] = ld(pin + i * P.plane + rs + xs, i);
     }
     if (P.g.bcmask != nullptr) {
       const uint32_t word = __ldg(P.g.bcmask + (int64_t)y * P.g.words + (x >> 5));
@@ -61,7 +73,7 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
         for (int i = 0; i < 9; ++i) {
           const uint32_t s = (d >> (2 * i)) & 3u;
           if (s == LBM_SRC_BOUNCE) {
-            const R v = St::ld(pin + opp(i) * P.plane + r0 + x, opp(i));
+            const R v = ld(pin + opp(i) * P.plane + r0 + x, opp(i));
             if (EXACT)
               f[i] = (R)__dsub_rn((double)v, P.g.kconst[ks][i]);
             else
@@ -163,31 +175,32 @@ __global__ void __launch_bounds__(256) lattice_kernel(const __grid_constant__ KP
   const uint32_t skip = P.g.pressure ? ((x == 0 ? P.g.pin : 0u) | (x == nx - 1 ? P.g.pout : 0u)) : 0u;
 #pragma unroll
   for (int i = 0; i < 9; ++i)
-    if (!((skip >> i) & 1u)) St::st(pout + i * P.plane + r0 + x, f[i], i);
+    if (!((skip >> i) & 1u)) st(pout + i * P.plane + r0 + x, f[i], i);
   if (pressure_src) {
     if (x == nx - 2) {
 #pragma unroll
       for (int i = 0; i < 9; ++i)
-        if ((P.g.pin >> i) & 1u) St::st(pout + i * P.plane + r0 + 0, pin_v[i], i);
+        if ((P.g.pin >> i) & 1u) st(pout + i * P.plane + r0 + 0, pin_v[i], i);
     }
     if (x == 1) {
 #pragma unroll
       for (int i = 0; i < 9; ++i)
-        if ((P.g.pout >> i) & 1u) St::st(pout + i * P.plane + r0 + (nx - 1), pout_v[i], i);
+        if ((P.g.pout >> i) & 1u) st(pout + i * P.plane + r0 + (nx - 1), pout_v[i], i);
     }
   }
 }
 
-// the float32 and 16-bit storages: registers capped so that 1024 threads fit on an SM
-template <int STORE, int NPT, int THREADS, bool HAS_BC, bool HAS_PRESSURE>
+// the float32 and 16-bit storages: registers capped so that 1024 threads fit
+// on an SM; SHIFT: the reference-shifted 16-bit storages
+template <int STORE, int NPT, int THREADS, bool SHIFT, bool HAS_BC, bool HAS_PRESSURE>
 __global__ void __launch_bounds__(THREADS, (STORE == LBM_STORE_F16S || STORE == LBM_STORE_BF16S ||
                                             (STORE == LBM_STORE_F32 && NPT <= 2))
                                                ? 1024 / THREADS
                                                : 1)
     fused_v2_kernel(const __grid_constant__ KParams P) {
-  fused_v2_body<STORE, NPT, HAS_BC, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out,
-                                                  (blockIdx.x * THREADS + threadIdx.x) * NPT, blockIdx.y,
-                                                  launch_seed(P));
+  fused_v2_body<STORE, NPT, HAS_BC, HAS_PRESSURE, false, SHIFT>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out,
+                                                                (blockIdx.x * THREADS + threadIdx.x) * NPT,
+                                                                blockIdx.y, launch_seed(P));
 }
 
 // one node per thread: registers capped so that 1024 threads fit on an SM
@@ -201,7 +214,7 @@ __global__ void __launch_bounds__(THREADS, NPT == 1 ? 1024 / THREADS : 1) fused_
 // over every node, one thread per listed boundary node recomputes that node
 // with its sources (the same body at one node per thread, so the arithmetic and
 // the random bits are those of the in-step path) and overwrites its outputs.
-template <int STORE, int THREADS, bool HAS_PRESSURE>
+template <int STORE, int THREADS, bool HAS_PRESSURE, bool SHIFT>
 __global__ void __launch_bounds__(THREADS) fixup_v2_kernel(const __grid_constant__ KParams P) {
   const int t = blockIdx.x * THREADS + threadIdx.x;
   if (t >= P.g.n_bcnodes) return;
@@ -210,8 +223,8 @@ __global__ void __launch_bounds__(THREADS) fixup_v2_kernel(const __grid_constant
   if constexpr (STORE == LBM_STORE_FX64)
     fused_fx_body<1, true, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out, x, y);
   else
-    fused_v2_body<STORE, 1, true, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out, x, y,
-                                                launch_seed(P));
+    fused_v2_body<STORE, 1, true, HAS_PRESSURE, false, SHIFT>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out, x, y,
+                                                              launch_seed(P));
 }
 
 // adds the steps of a lbm_lattice_run_opts call to its device step counter
@@ -247,6 +260,13 @@ static int dispatch(int storage, bool exact, const KParams& P, cudaStream_t s) {
     case LBM_STORE_F16S: return launch<LBM_STORE_F16S, false, MODE>(P, s);
     case LBM_STORE_BF16S: return launch<LBM_STORE_BF16S, false, MODE>(P, s);
     case LBM_STORE_FX64: return launch<LBM_STORE_FX64, false, MODE>(P, s);
+    case LBM_STORE_F16R:
+    case LBM_STORE_BF16R: {
+      KParams Q = P;
+      Q.dev_shift = 1;
+      return storage == LBM_STORE_F16R ? launch<LBM_STORE_F16S, false, MODE>(Q, s)
+                                       : launch<LBM_STORE_BF16S, false, MODE>(Q, s);
+    }
     default: return set_error(LBM_ERR_ARG, "unknown storage type");
   }
 }
@@ -273,10 +293,10 @@ static dim3 v2_grid(const KParams& P) {
   return dim3((unsigned)((chunks + kV2Threads - 1) / kV2Threads), (unsigned)P.g.ny, 1);
 }
 
-template <int STORE, int NPT>
+template <int STORE, int NPT, bool SHIFT = false>
 static int launch_v2(const KParams& P, cudaStream_t s) {
   const dim3 grid = v2_grid<NPT>(P);
-  LBM_LAUNCH_SPECIALISED(fused_v2_kernel, STORE, NPT, kV2Threads);
+  LBM_LAUNCH_SPECIALISED(fused_v2_kernel, STORE, NPT, kV2Threads, SHIFT);
   count_launch();
   return check_launch("fused_v2_kernel");
 }
@@ -299,10 +319,13 @@ static int default_npt(int storage) {
   }
 }
 
+// the reference-shifted 16-bit storages run at 4 nodes per thread only
+static bool ref_shifted(int storage) { return storage == LBM_STORE_F16R || storage == LBM_STORE_BF16R; }
+
 // nodes per thread of the vectorised kernel for this lattice, 0 when it does not apply
 static int v2_npt(int storage, int flags, const KParams& P) {
   if ((flags & LBM_FLAG_EXACT) || (flags & LBM_FLAG_GENERIC)) return 0;
-  int npt = (flags >> LBM_FLAG_NPT_SHIFT) & 15;
+  int npt = ref_shifted(storage) ? 0 : (flags >> LBM_FLAG_NPT_SHIFT) & 15;
   if (npt == 0) npt = default_npt(storage);
   if (!v2_fits(P, npt)) return 0;
   return npt;
@@ -310,13 +333,13 @@ static int v2_npt(int storage, int flags, const KParams& P) {
 
 constexpr int kFixupThreads = 128;
 
-template <int STORE>
+template <int STORE, bool SHIFT = false>
 static int launch_fixup(const KParams& P, cudaStream_t s) {
   const dim3 grid((unsigned)((P.g.n_bcnodes + kFixupThreads - 1) / kFixupThreads));
   if (P.g.pressure)
-    fixup_v2_kernel<STORE, kFixupThreads, true><<<grid, kFixupThreads, 0, s>>>(P);
+    fixup_v2_kernel<STORE, kFixupThreads, true, SHIFT><<<grid, kFixupThreads, 0, s>>>(P);
   else
-    fixup_v2_kernel<STORE, kFixupThreads, false><<<grid, kFixupThreads, 0, s>>>(P);
+    fixup_v2_kernel<STORE, kFixupThreads, false, SHIFT><<<grid, kFixupThreads, 0, s>>>(P);
   count_launch();
   return check_launch("fixup_v2_kernel");
 }
@@ -333,7 +356,8 @@ static int launch_fused_step(int storage, int npt, int flags, const KParams& P, 
 // lose below 2048^2 (64 against 85 at 1024^2); the other storages gain only at
 // 8192^2 (fx64 46.9 against 46.5) and lose or tie up to 4096^2.
 static int64_t split_nodes(int storage) {
-  return (storage == LBM_STORE_F16S || storage == LBM_STORE_BF16S) ? (int64_t)1 << 22 : (int64_t)1 << 25;
+  return (storage == LBM_STORE_F16S || storage == LBM_STORE_BF16S || ref_shifted(storage)) ? (int64_t)1 << 22
+                                                                                              : (int64_t)1 << 25;
 }
 
 static int launch_fused(int storage, int flags, const KParams& P, cudaStream_t s) {
@@ -354,6 +378,8 @@ static int launch_fused(int storage, int flags, const KParams& P, cudaStream_t s
     case LBM_STORE_F16S: return launch_fixup<LBM_STORE_F16S>(P, s);
     case LBM_STORE_BF16S: return launch_fixup<LBM_STORE_BF16S>(P, s);
     case LBM_STORE_FX64: return launch_fixup<LBM_STORE_FX64>(P, s);
+    case LBM_STORE_F16R: return launch_fixup<LBM_STORE_F16S, true>(P, s);
+    case LBM_STORE_BF16R: return launch_fixup<LBM_STORE_BF16S, true>(P, s);
     default: return set_error(LBM_ERR_ARG, "unknown storage type");
   }
 }
@@ -373,6 +399,8 @@ static int launch_fused_step(int storage, int npt, int flags, const KParams& P, 
     case LBM_STORE_BF16S * 16 + 2: return launch_v2<LBM_STORE_BF16S, 2>(P, s);
     case LBM_STORE_BF16S * 16 + 4: return launch_v2<LBM_STORE_BF16S, 4>(P, s);
     case LBM_STORE_BF16S * 16 + 8: return launch_v2<LBM_STORE_BF16S, 8>(P, s);
+    case LBM_STORE_F16R * 16 + 4: return launch_v2<LBM_STORE_F16S, 4, true>(P, s);
+    case LBM_STORE_BF16R * 16 + 4: return launch_v2<LBM_STORE_BF16S, 4, true>(P, s);
     default: return dispatch<MODE_FUSED>(storage, flags & LBM_FLAG_EXACT, P, s);
   }
 }
@@ -383,7 +411,9 @@ static size_t store_bytes(int storage) {
     case LBM_STORE_FX64: return 8;
     case LBM_STORE_F32: return 4;
     case LBM_STORE_F16S:
-    case LBM_STORE_BF16S: return 2;
+    case LBM_STORE_BF16S:
+    case LBM_STORE_F16R:
+    case LBM_STORE_BF16R: return 2;
     default: return 0;
   }
 }
@@ -427,6 +457,7 @@ int lbm_lattice_init(const lbm_geometry* g, int32_t storage, const double* f, co
     P.u_in = ref_u(u, g->ny);
   }
   P.omega = omega;
+  set_shift(P);
   return dispatch<MODE_INIT>(storage, flags & LBM_FLAG_EXACT, P, (cudaStream_t)stream);
 }
 
@@ -467,6 +498,7 @@ int lbm_lattice_run_opts(const lbm_geometry* g, int32_t storage, void* pop_a, vo
   P.pitch = pitch;
   P.plane = pitch * g->ny;
   P.omega = omega;
+  set_shift(P);
   P.sr = (flags & LBM_FLAG_STOCHASTIC) != 0;
   P.qc = fx::q_consts(omega);
   P.step_dev = counter;
@@ -506,6 +538,7 @@ int lbm_lattice_read(const lbm_geometry* g, int32_t storage, const void* pop, in
   P.f_out = ref_f_out(f_out, g->ny);
   P.rho_out = ref_rho_out(rho_out, g->ny);
   P.u_out = ref_u_out(u_out, g->ny);
+  set_shift(P);  // omega 1: the read converts, it does not collide
   return dispatch<MODE_READ>(storage, false, P, (cudaStream_t)stream);
 }
 

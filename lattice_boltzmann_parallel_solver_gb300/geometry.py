@@ -18,6 +18,7 @@ fixed populations go into two small tables passed by value to the kernels.
 """
 from __future__ import annotations
 
+import copy
 import ctypes
 
 import numpy as np
@@ -152,6 +153,16 @@ class CompiledGeometry:
     @property
     def ref(self):
         return ctypes.byref(self.struct)
+
+    def with_dev_ref(self, ux: float, uy: float) -> "CompiledGeometry":
+        """This geometry with the reference velocity of the reference-shifted
+        16-bit storages ("f16r", "bf16r") set to (ux, uy): a copy of the
+        descriptor struct that shares the device arrays."""
+        assert abs(ux) < 0.5 and abs(uy) < 0.5, "the reference velocity must lie inside (-0.5, 0.5)"
+        g = copy.copy(self)
+        g.struct = _lib.Geometry.from_buffer_copy(self.struct)
+        g.struct.dev_ref_ux, g.struct.dev_ref_uy = float(ux), float(uy)
+        return g
 
 
 _EMPTY = {}

@@ -3,7 +3,7 @@
 
 The populations live on the device as structure-of-arrays planes
 pop[9][ny][pitch] (x contiguous, pitch a multiple of 32 elements) in one of
-five storage forms:
+seven storage forms:
 
   "fx64"  round((f_i - w_i) 2^56) in int64, exact integer moments and
           linear relaxation, float-float quadratic term: float64 accuracy
@@ -12,6 +12,10 @@ five storage forms:
   "f32"   float32 storage and arithmetic (36 B)
   "f16"   float32 arithmetic, f_i - w_i stored in binary16 (18 B)
   "bf16"  float32 arithmetic, f_i - w_i stored in bfloat16 (18 B)
+  "f16r", "bf16r"  as "f16" / "bf16" with w_i replaced by c_i, the
+          equilibrium at rho = 1 and a reference velocity (``dev_ref``): a
+          flow near a uniform velocity (a channel at its inlet velocity) keeps
+          smaller stored deviations and smaller rounding errors
 
 One fused kernel per step reads the previous post-collision populations
 once, streams them by pulling, applies the boundary descriptor, forms the
@@ -34,8 +38,26 @@ STORAGES = {
     "f32": (_lib.STORE_F32, torch.float32, torch.float32),
     "f16": (_lib.STORE_F16S, torch.float16, torch.float32),
     "bf16": (_lib.STORE_BF16S, torch.bfloat16, torch.float32),
+    "f16r": (_lib.STORE_F16R, torch.float16, torch.float32),
+    "bf16r": (_lib.STORE_BF16R, torch.bfloat16, torch.float32),
 }
-BYTES_PER_NODE = {"fx64": 144, "f64": 144, "f32": 72, "f16": 36, "bf16": 36}
+BYTES_PER_NODE = {"fx64": 144, "f64": 144, "f32": 72, "f16": 36, "bf16": 36, "f16r": 36, "bf16r": 36}
+# the storages that keep 16-bit deviations (stochastic rounding on by default)
+SIXTEEN_BIT = ("f16", "bf16", "f16r", "bf16r")
+# the reference-shifted ones
+REF_SHIFTED = ("f16r", "bf16r")
+
+
+def with_dev_ref(geo, storage: str, dev_ref):
+    """The geometry to pass with ``storage``: for the reference-shifted
+    storages a copy carrying the reference velocity ``dev_ref`` (default
+    (0, 0)); the geometry itself otherwise, where ``dev_ref`` must be None."""
+    if storage in REF_SHIFTED:
+        ux, uy = dev_ref if dev_ref is not None else (0.0, 0.0)
+        return geo.with_dev_ref(ux, uy)
+    if dev_ref is not None:
+        raise ValueError("dev_ref applies to the reference-shifted storages %s only" % (REF_SHIFTED,))
+    return geo
 
 
 class Lattice:
@@ -44,7 +66,7 @@ class Lattice:
     def __init__(self, nx: int, ny: int, omega: float, boundary=None, storage: str = None,
                  exact: bool = False, device: str = "cuda", generic: bool = False, npt: int = 0,
                  stochastic: bool = None, seed: int = 0, bc_inline: bool | None = None,
-                 probe: tuple = None, probe_cap: int = 0):
+                 probe: tuple = None, probe_cap: int = 0, dev_ref: tuple = None):
         """``generic`` forces the one-node-per-thread kernel; ``npt`` sets the
         nodes per thread of the vectorised kernel (0 = the default for the storage).
         ``stochastic`` (default: on for the 16-bit storages) rounds the stored
@@ -59,7 +81,9 @@ class Lattice:
         float64 operation order, bit for bit).  ``probe`` = (x, y) records the
         velocity of that node at every fused step, up to ``probe_cap`` steps
         (``probe_trace``): the per-step probe of the reference's drivers
-        (src/experiments.py:690,703-704) kept on the device."""
+        (src/experiments.py:690,703-704) kept on the device.  ``dev_ref`` =
+        (ux, uy): the reference velocity of the "f16r" / "bf16r" storages
+        (default (0, 0)); they run at 4 nodes per thread (``npt`` ignored)."""
         A.require_cuda()
         assert 0 < omega < 2
         if storage is None:
@@ -70,7 +94,7 @@ class Lattice:
         self.storage = storage
         self.store_id, self.pop_dtype, self.aux_dtype = STORAGES[storage]
         if stochastic is None:
-            stochastic = storage in ("f16", "bf16")
+            stochastic = storage in SIXTEEN_BIT
         self.flags = (_lib.FLAG_EXACT if exact else 0) | (_lib.FLAG_GENERIC if generic else 0) | \
             ((int(npt) & 15) << _lib.FLAG_NPT_SHIFT) | (_lib.FLAG_STOCHASTIC if stochastic else 0) | \
             {True: _lib.FLAG_BC_INLINE, False: _lib.FLAG_BC_SPLIT}.get(bc_inline, 0)
@@ -79,6 +103,8 @@ class Lattice:
         self.device = torch.device(device)
         self.boundary = boundary
         self.geo = boundary.geometry(self.nx, self.ny) if boundary is not None else empty_geometry(self.nx, self.ny)
+        self.geo = with_dev_ref(self.geo, storage, dev_ref)
+        self.dev_ref = None if storage not in REF_SHIFTED else (self.geo.struct.dev_ref_ux, self.geo.struct.dev_ref_uy)
         if not self.geo.fusable:
             raise NotImplementedError("the outlet must sit on column nx-1 for the resident lattice")
         n = 9 * self.ny * self.pitch

@@ -24,6 +24,7 @@ import torch
 from . import boundary_utils as BU
 from . import scenarios as S
 from .batch import Batch, Member
+from .lattice import REF_SHIFTED
 
 
 @dataclass
@@ -41,6 +42,7 @@ class Request:
     arrival: float = 0.0          # seconds after the stream starts
     params: dict = field(default_factory=dict)
     init: object = None           # () -> (f0, rho0, u0): the initial state built on demand
+    dev_ref: tuple = None         # reference velocity for the "f16r" / "bf16r" storages (default (0, 0))
     # filled in by the engine
     prepared: tuple = None        # the initial state on the device, built while the GPU runs a tick
     admitted: float = None
@@ -103,7 +105,8 @@ def request_mix(n, rate=50.0, seed=7, step_range=(1000, 50000), kinds=("couette"
     up to 2048 x 512) and the von Karman channel (420 x 180, Re 100); the same
     requests at every rate (``request_stream``).  With ``lazy`` the initial
     states are built on the device at admission (long streams would not fit
-    the host memory up front)."""
+    the host memory up front).  The channel requests carry their inlet velocity
+    as the reference of the reference-shifted storages."""
     out = []
     for rid, t, kind, steps, nx, ny, params in request_stream(n, rate, seed, step_range, kinds):
         if kind == "couette":
@@ -120,7 +123,8 @@ def request_mix(n, rate=50.0, seed=7, step_range=(1000, 50000), kinds=("couette"
             om = 1.0 / (3.0 * (0.1 * 40 / 100.0) + 0.5)
             bnd = BU.von_karman_boundary_conditions(420, 180, 1.0, 0.1, 40, walls=True, plate_offset=1)
             req = Request(rid, kind, 420, 180, om, steps, bnd, None, None, None, t, params,
-                          init=lambda rid=rid: S.von_karman_start(420, 180, 0.1, 1e-3, seed=rid))
+                          init=lambda rid=rid: S.von_karman_start(420, 180, 0.1, 1e-3, seed=rid),
+                          dev_ref=(0.1, 0.0))
         if not lazy:
             req.f0, req.rho0, req.u0 = req.init()
         out.append(req)
@@ -183,7 +187,7 @@ class ServingEngine:
                                    for t in state)
 
     def state_bytes(self, req):
-        per = {"fx64": 8, "f64": 8, "f32": 4, "f16": 2, "bf16": 2}[self.storage]
+        per = {"fx64": 8, "f64": 8, "f32": 4, "f16": 2, "bf16": 2, "f16r": 2, "bf16r": 2}[self.storage]
         pitch = (req.nx + 31) // 32 * 32
         return 2 * 9 * req.ny * pitch * per + 2 * 3 * req.ny * 8
 
@@ -213,7 +217,8 @@ class ServingEngine:
                 self._prepare([r])
                 main.wait_stream(self.side)
                 f0, rho0, u0 = r.prepared
-                m = b.add(Member(r.nx, r.ny, r.omega, r.boundary, steps=r.steps, f0=f0, rho0=rho0, u0=u0))
+                m = b.add(Member(r.nx, r.ny, r.omega, r.boundary, steps=r.steps, f0=f0, rho0=rho0, u0=u0,
+                                 dev_ref=r.dev_ref if self.storage in REF_SHIFTED else None))
                 # the first step has consumed the initial state (its memory, from
                 # the side stream's pool, is not reused before that step has run)
                 for t in r.prepared:

@@ -18,6 +18,7 @@ import torch
 from . import analysis
 from . import boundary_utils as BU
 from .batch import Batch, Member
+from .lattice import REF_SHIFTED
 
 PLATE = 40          # the plate size every sweep keeps (x_strouhal's default)
 
@@ -73,7 +74,9 @@ def strouhal_sweep(kind: str, values=None, steps: int = 200000, storage: str = "
     per point, its parameters, the |u| trace at (3 lx / 4, ly / 2) (the
     reference's vel_at_p: steps + 1 samples) and the Strouhal numbers
     St = f d / u with d = 40: by the reference's post-processing
-    (``strouhal_argmax``) and by the sub-bin estimate (``strouhal``)."""
+    (``strouhal_argmax``) and by the sub-bin estimate (``strouhal``).  With a
+    reference-shifted storage ("f16r", "bf16r") each point's reference velocity
+    is its inlet velocity."""
     pts = sweep_points(kind, values)
     members = []
     for p in pts:
@@ -82,7 +85,7 @@ def strouhal_sweep(kind: str, values=None, steps: int = 200000, storage: str = "
         bnd = BU.von_karman_boundary_conditions(lx, ly, 1.0, p["u"], PLATE)
         f0, rho0, u0 = _uniform_flow(lx, ly, p["u"], device)
         members.append(Member(lx, ly, omega, bnd, steps=steps, probe=(3 * lx // 4, ly // 2), f0=f0, rho0=rho0,
-                              u0=u0))
+                              u0=u0, dev_ref=(p["u"], 0.0) if storage in REF_SHIFTED else None))
     b = Batch(members, storage=storage, device=device).start()
     b.run_graph(chunk=chunk)
     out = []

@@ -142,3 +142,21 @@ def test_batch_argument_errors_without_gpu(lib):
         _lib.check(build())
     with pytest.raises(AssertionError, match="batch run"):
         _lib.check(lib.lbm_batch_run(ptr, 1, 10, -1, 2, 4, 64, None, 1, 0, None))
+
+
+def test_storage_constants_match_header():
+    text = open(HEADER).read()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"#define LBM_STORE_(\w+) (\d+)", text)}
+    assert defs == {"F64": _lib.STORE_F64, "F32": _lib.STORE_F32, "F16S": _lib.STORE_F16S,
+                    "BF16S": _lib.STORE_BF16S, "FX64": _lib.STORE_FX64, "F16R": _lib.STORE_F16R,
+                    "BF16R": _lib.STORE_BF16R}
+
+
+def test_reference_velocity_range_checked_without_gpu(lib):
+    g = _lib.Geometry()
+    g.nx, g.ny = 8, 4
+    for ux, uy in ((0.5, 0.0), (0.0, -0.7), (float("nan"), 0.0)):
+        g.dev_ref_ux, g.dev_ref_uy = ux, uy
+        with pytest.raises(AssertionError, match="reference velocity"):
+            _lib.check(lib.lbm_lattice_run(ctypes.byref(g), _lib.STORE_F16R, 1, 2, 32, None, None, 1.0, 1, None,
+                                           None, 0, 0, None))

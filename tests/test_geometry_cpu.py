@@ -218,3 +218,19 @@ def test_von_karman_channel_form(offset):
     want = O.von_karman_boundary(lx, ly, 1.0, 0.1, d, walls=True, plate_offset=offset)(pre, post.copy(), None,
                                                                                          None, prev)
     assert np.array_equal(got, want)
+
+
+def test_reference_velocity_copy_shares_the_descriptor():
+    from lattice_boltzmann_parallel_solver_gb300.lattice import with_dev_ref
+    geo = compiled(BU.couette_flow_boundary_conditions(60, 30, 0.05, 1.0), 60, 30)
+    r = with_dev_ref(geo, "f16r", (0.1, -0.02))
+    assert (r.struct.dev_ref_ux, r.struct.dev_ref_uy) == (0.1, -0.02)
+    assert (geo.struct.dev_ref_ux, geo.struct.dev_ref_uy) == (0.0, 0.0)
+    assert r.desc is geo.desc and r.struct.desc == geo.struct.desc and r.struct.n_bcnodes == geo.struct.n_bcnodes
+    z = with_dev_ref(geo, "bf16r", None)
+    assert (z.struct.dev_ref_ux, z.struct.dev_ref_uy) == (0.0, 0.0)
+    assert with_dev_ref(geo, "f16", None) is geo
+    with pytest.raises(ValueError):
+        with_dev_ref(geo, "f16", (0.1, 0.0))
+    with pytest.raises(AssertionError):
+        with_dev_ref(geo, "f16r", (0.6, 0.0))
