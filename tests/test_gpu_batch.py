@@ -105,7 +105,7 @@ def test_autotune_picks_a_working_config(pkg):
         assert float((b.read(j)[0] - ref).abs().max()) <= 1e-6
 
 
-@pytest.mark.parametrize("storage", ["fx64", "f64", "f32", "f16", "bf16"])
+@pytest.mark.parametrize("storage", ["fx64", "f64", "f32", "f16", "bf16", "f16r"])
 def test_boundary_node_pass_equals_inline_sources(pkg, storage):
     """The default batched step (a boundary-free launch, then the pass over the
     listed boundary nodes) gives bit-identical states and probe traces to the
@@ -114,13 +114,16 @@ def test_boundary_node_pass_equals_inline_sources(pkg, storage):
     an inlet node and a pressure-column node, which the pass records."""
     from lattice_boltzmann_parallel_solver_gb300.batch import Batch
     npt = {"fx64": 1, "f64": 2, "f32": 2}.get(storage, 4)
+    threads = 128 if storage == "f16r" else 64  # the reference-shifted storages run at 128 threads
     runs = []
     for inline in (True, False):
         ms = members(pkg, steps=(40, 33, 40, 40, 40))
         ms[1].probe = (0, 20)
         ms[2].probe = (18, 36)
         ms[3].probe = (48, 9)
-        b = Batch(ms, storage=storage, npt=npt, threads=64, rows=2, inline_bc=inline).start()
+        if storage == "f16r":
+            ms[0].dev_ref = (0.1, 0.0)
+        b = Batch(ms, storage=storage, npt=npt, threads=threads, rows=2, inline_bc=inline).start()
         assert (b.bc_chunks == -1) == inline and (inline or b.bc_chunks > 0)
         b.run()
         runs.append((b, ms))
