@@ -214,8 +214,10 @@ inline int64_t pass_nodes(const GeoK& g) {
   return (g.bcmask != nullptr ? (int64_t)(g.n_bcnodes - g.n_bcnodes_edge) : 0) + (g.pressure ? 2 * (int64_t)g.ny : 0);
 }
 
+// 64 registers: 8 blocks of the latency-bound pass per SM (f16 takes 66
+// without the cap, 7 blocks); the fixed-point body would spill under it
 template <int STORE, bool SHIFT>
-__global__ void __launch_bounds__(kFixupChunk)
+__global__ void __launch_bounds__(kFixupChunk, STORE == LBM_STORE_FX64 ? 1 : 8)
     batch_fixup_kernel(const BatchEntry* __restrict__ tab, const int* __restrict__ bc_start, int n_inst,
                        const int* __restrict__ gbase, int k) {
   __shared__ __align__(16) unsigned char ebuf[sizeof(BatchEntry)];
@@ -253,8 +255,11 @@ __global__ void __launch_bounds__(kFixupChunk)
     else fused_fx_body<1, true, false>(e.P, pin, pout, ain, aout, x, y);
   } else {
     const uint32_t seed = hash32(e.P.seed + (uint32_t)(g - e.s0));
-    if (e.P.g.pressure) fused_v2_body<STORE, 1, true, true, false, SHIFT>(e.P, pin, pout, ain, aout, x, y, seed);
-    else fused_v2_body<STORE, 1, true, false, false, SHIFT>(e.P, pin, pout, ain, aout, x, y, seed);
+    const bool in_list = t < listed;
+    if (e.P.g.pressure)
+      fused_v2_body<STORE, 1, true, true, false, SHIFT>(e.P, pin, pout, ain, aout, x, y, seed, in_list);
+    else
+      fused_v2_body<STORE, 1, true, false, false, SHIFT>(e.P, pin, pout, ain, aout, x, y, seed, in_list);
   }
 }
 

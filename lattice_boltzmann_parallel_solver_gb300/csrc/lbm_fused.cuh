@@ -124,7 +124,7 @@ __device__ __forceinline__ void write_probe(const KParams& P, int x, int y, R ux
 template <int STORE, int NPT, bool HAS_BC, bool HAS_PRESSURE, bool EDGES = false, bool SHIFT = false>
 __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_in_v, void* pop_out_v,
                                               const void* aux_in_v, void* aux_out_v, int x0, int y,
-                                              uint32_t seed) {
+                                              uint32_t seed, bool listed = false) {
   using St = Store<STORE>;
   using T = typename St::T;
   using R = typename St::R;
@@ -175,9 +175,17 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     else return SH ? fma(v, R(1) / kS, wr<R>(i)) : v;
   };
 
-  // the boundary mask word first: its latency overlaps the population loads
+  // the boundary mask word first: its latency overlaps the population loads.
+  // The boundary-node pass on a node of the boundary list (listed) knows its
+  // bit: its descriptor and its own populations (the bounce-back sources) then
+  // load together with the pulled ones instead of one after another.
   const bool has_bc = HAS_BC && P.g.bcmask != nullptr;
-  const uint32_t bcword = has_bc ? __ldg(P.g.bcmask + y * P.g.words + (x0 >> 5)) : 0u;
+  constexpr bool PASS = NPT == 1 && HAS_BC;
+  const bool known = PASS && has_bc && listed;
+  const uint32_t bcword =
+      has_bc ? (known ? (1u << (x0 & 31)) : __ldg(P.g.bcmask + y * P.g.words + (x0 >> 5))) : 0u;
+  const uint32_t dknown = known ? __ldg(P.g.desc + y * nx + x0) : 0u;
+  R own[PASS ? 9 : 1];
   R f[9][NPT];
 #pragma unroll
   for (int i = 0; i < 9; ++i) {
@@ -186,6 +194,7 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
     if constexpr (NPT == 1) {
       // one node per thread (the boundary-node pass): neighbours loaded directly
       f[i][0] = ld_work(base + (cx(i) == 1 ? xm : (cx(i) == -1 ? xp : x0)), i);
+      if constexpr (PASS) own[i] = ld_work(pin + i * plane + r0 + x0, i);
       continue;
     }
     T raw[NPT];
@@ -248,13 +257,16 @@ __device__ __forceinline__ void fused_v2_body(const KParams& P, const void* pop_
       for (int k = 0; k < NPT; ++k) {
         if (!((bits >> k) & 1u)) continue;
         const int x = x0 + k;
-        const uint32_t d = __ldg(P.g.desc + y * nx + x);
+        const uint32_t d = known ? dknown : __ldg(P.g.desc + y * nx + x);
         const int ks = (d >> LBM_DESC_KSET_SHIFT) & 15, cs = (d >> LBM_DESC_CSET_SHIFT) & 15;
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
           const uint32_t s = (d >> (2 * i)) & 3u;
           if (s == LBM_SRC_BOUNCE) {
-            R v = ld_work(pin + opp(i) * plane + r0 + x, opp(i)) - (R)P.g.kconst[ks][i] * kS;
+            R v;
+            if constexpr (PASS) v = own[opp(i)];
+            else v = ld_work(pin + opp(i) * plane + r0 + x, opp(i));
+            v -= (R)P.g.kconst[ks][i] * kS;
             if constexpr (SHIFT) v += sig(opp(i)) - sig(i);
             f[i][k] = v;
           } else if (s == LBM_SRC_CONST)

@@ -224,7 +224,7 @@ __global__ void __launch_bounds__(THREADS) fixup_v2_kernel(const __grid_constant
     fused_fx_body<1, true, HAS_PRESSURE>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out, x, y);
   else
     fused_v2_body<STORE, 1, true, HAS_PRESSURE, false, SHIFT>(P, P.pop_in, P.pop_out, P.aux_in, P.aux_out, x, y,
-                                                              launch_seed(P));
+                                                              launch_seed(P), true);
 }
 
 // adds the steps of a lbm_lattice_run_opts call to its device step counter
