@@ -104,7 +104,7 @@ typedef struct lbm_geometry {
  * A flow near a uniform velocity (a channel at its inlet velocity) then keeps
  * smaller stored deviations and smaller rounding errors.  The vectorised
  * kernels run them at 4 nodes per thread (the LBM_FLAG_NPT field is ignored)
- * and the batched step at npt 4 and 128 threads. */
+ * and the batched step at npt 2 or 4 and 128 threads. */
 #define LBM_STORE_F16R 5  /* 18 B per node, 1024 (f_i - c_i) in binary16 */
 #define LBM_STORE_BF16R 6 /* 18 B per node, f_i - c_i in bfloat16 */
 

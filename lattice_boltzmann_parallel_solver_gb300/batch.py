@@ -71,7 +71,7 @@ class Batch:
         plain grid of one tile per block, 0 persistent blocks filling the GPU
         that walk contiguous spans of tiles, any other number that many
         persistent blocks.  The reference-shifted storages ("f16r", "bf16r",
-        each member's ``dev_ref``) run at 4 x 128 only."""
+        each member's ``dev_ref``) run at 128 threads and 2 or 4 nodes per thread."""
         A.require_cuda()
         self.stochastic = storage in SIXTEEN_BIT if stochastic is None else bool(stochastic)
         self.storage = storage
@@ -153,10 +153,10 @@ class Batch:
         launch per step, boundary sources inside, row-segment tiles) 2 x 128
         for the 16-bit storages and 1 x 128 for fx64; above (boundary-free step
         over runs across row ends, then the boundary-node pass) 4 x 128 and
-        1 x 64; 4 x 128 always for the reference-shifted storages."""
+        1 x 64 (the reference-shifted 16-bit storages as the others)."""
         split = self.inline_bc is False or (self.inline_bc is None and nodes >= (1 << 20))
         if self._auto_shape[0]:
-            self.npt = {"fx64": 1, "f64": 2, "f16": 4 if split else 2, "bf16": 4 if split else 2}.get(self.storage, 4)
+            self.npt = {"fx64": 1, "f64": 2}.get(self.storage, 4 if split or self.storage == "f32" else 2)
         if self._auto_shape[1]:
             self.threads = {"fx64": 64 if split else 128}.get(self.storage, 128)
 
@@ -293,8 +293,7 @@ def autotune(batch: Batch, candidates=None, steps: int = 6, warmup: int = 2):
     (probes off) and the global step counter is reset afterwards."""
     sms = torch.cuda.get_device_properties(batch.device).multi_processor_count
     if candidates is None:
-        npts = {"fx64": (1, 2), "f16": (2, 4, 8), "bf16": (2, 4, 8), "f16r": (4,), "bf16r": (4,)}.get(
-            batch.storage, (2, 4))
+        npts = {"fx64": (1, 2), "f16": (2, 4, 8), "bf16": (2, 4, 8)}.get(batch.storage, (2, 4))
         threads = (128,) if batch.storage in REF_SHIFTED else (64, 128, 256)
         candidates = [(p, t, b, r) for p in npts for t in threads for b in (0, 8 * sms, ONE_TILE_PER_BLOCK)
                       for r in (1, 2, 4, 8, 16)]

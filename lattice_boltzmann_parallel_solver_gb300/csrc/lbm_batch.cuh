@@ -332,17 +332,19 @@ int batch_launch_split(const void* table, int n, int tiles, int bc_chunks, int s
     LBM_BATCH_NPT(LBM_STORE_BF16S, 2, HAS_BC)                                                                \
     LBM_BATCH_NPT(LBM_STORE_BF16S, 4, HAS_BC)                                                                \
     LBM_BATCH_NPT(LBM_STORE_BF16S, 8, HAS_BC)                                                                \
-    if (storage == LBM_STORE_F16R && npt == 4 && threads == 128)                                             \
-      return launch_batch<LBM_STORE_F16S, 4, 128, HAS_BC, true>(table, n, tiles, bc_chunks, gbase, nsteps,   \
-                                                                blocks, s);                                  \
-    if (storage == LBM_STORE_BF16R && npt == 4 && threads == 128)                                            \
-      return launch_batch<LBM_STORE_BF16S, 4, 128, HAS_BC, true>(table, n, tiles, bc_chunks, gbase, nsteps,  \
-                                                                 blocks, s);                                 \
+    LBM_BATCH_REF(LBM_STORE_F16R, LBM_STORE_F16S, 2, HAS_BC)                                                 \
+    LBM_BATCH_REF(LBM_STORE_F16R, LBM_STORE_F16S, 4, HAS_BC)                                                 \
+    LBM_BATCH_REF(LBM_STORE_BF16R, LBM_STORE_BF16S, 2, HAS_BC)                                               \
+    LBM_BATCH_REF(LBM_STORE_BF16R, LBM_STORE_BF16S, 4, HAS_BC)                                               \
     return set_error(LBM_ERR_UNSUPPORTED, "no batched kernel for this storage / npt / threads");              \
   } while (0)
 #define LBM_BATCH_CASE(ST, NP, TH, HAS_BC)               \
   if (storage == ST && npt == NP && threads == TH)       \
     return launch_batch<ST, NP, TH, HAS_BC>(table, n, tiles, bc_chunks, gbase, nsteps, blocks, s);
+// the reference-shifted storages: 128 threads only
+#define LBM_BATCH_REF(ST, BASE, NP, HAS_BC)                  \
+  if (storage == ST && npt == NP && threads == 128)          \
+    return launch_batch<BASE, NP, 128, HAS_BC, true>(table, n, tiles, bc_chunks, gbase, nsteps, blocks, s);
 #define LBM_BATCH_NPT(ST, NP, HAS_BC) \
   LBM_BATCH_CASE(ST, NP, 64, HAS_BC) LBM_BATCH_CASE(ST, NP, 128, HAS_BC) LBM_BATCH_CASE(ST, NP, 256, HAS_BC)
 
