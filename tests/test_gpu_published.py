@@ -126,15 +126,23 @@ def test_vk_strouhal_against_published(pkg, pub, storage, tol):
     assert err <= tol
 
 
-def test_reynolds_sweep_against_published(pkg, pub):
+@pytest.mark.parametrize("storage", ["fx64", "f16r"])
+def test_reynolds_sweep_against_published(pkg, pub, storage):
     """The Reynolds sweep of src/main.py:150-177 (Re 40 ... 200, 200 000 steps each)
-    as one batch in fx64: each point's Strouhal number by the reference's
-    post-processing lands within one FFT bin of the published one, and by the
-    sub-bin estimate within 1 %."""
+    as one batch in fx64, and in the reference-shifted f16 storage with each
+    point's inlet velocity as its reference: each point's Strouhal number by the
+    reference's post-processing lands within one FFT bin of the published one,
+    and by the sub-bin estimate within 1 %.  The float32-arithmetic storages
+    run Re 40 ... 170: at Re 200 (inlet 0.15, local |u| up to 0.33, omega 1.69)
+    the BGK step sits at its stability edge in float32, where perturbing the
+    inlet velocity by 1e-6 decides whether a run blows up (in the vectorised
+    and the one-node-per-thread kernels alike); fx64 runs all six points."""
     from lattice_boltzmann_parallel_solver_gb300 import sweeps
-    res = sweeps.strouhal_sweep("reynolds", steps=200000, storage="fx64")
-    assert [r["label"] for r in res] == list(pub["re_sweep_re"])
-    for r, st_a, st_i in zip(res, pub["re_sweep_st_argmax"], pub["re_sweep_st_interp"]):
+    values = None if storage == "fx64" else (40, 70, 100, 140, 170)
+    res = sweeps.strouhal_sweep("reynolds", values=values, steps=200000, storage=storage)
+    n = len(res)
+    assert [r["label"] for r in res] == list(pub["re_sweep_re"])[:n]
+    for r, st_a, st_i in zip(res, pub["re_sweep_st_argmax"][:n], pub["re_sweep_st_interp"][:n]):
         assert r["start"] in pub["re_sweep_start"]
         print("Re %d: St %.5f (published %.5f), argmax %.5f (published %.5f, bin %.5f)" % (
             r["label"], r["strouhal"], st_i, r["strouhal_argmax"], st_a, r["strouhal_bin"]))

@@ -44,14 +44,18 @@ def _rebuild(pkg, r):
 
 def clone(r, rid, arrival):
     from lattice_boltzmann_parallel_solver_gb300.serving import Request
-    return Request(rid, r.kind, r.nx, r.ny, r.omega, r.steps, r.boundary, r.f0, r.rho0, r.u0, arrival, dict(r.params))
+    return Request(rid, r.kind, r.nx, r.ny, r.omega, r.steps, r.boundary, r.f0, r.rho0, r.u0, arrival, dict(r.params),
+                   dev_ref=r.dev_ref)
 
 
-@pytest.mark.parametrize("storage", ["f16", "fx64"])
+@pytest.mark.parametrize("storage", ["f16", "fx64", "f16r"])
 def test_same_result_alone_and_in_mix(pkg, storage):
+    """(f16r: the request carries its own reference velocity, the others the default.)"""
     from lattice_boltzmann_parallel_solver_gb300.serving import ServingEngine
     reqs = small_mix(pkg)
     target = reqs[3]
+    if storage == "f16r":
+        target.dev_ref = (0.03, 0.0)
     alone = ServingEngine(storage=storage, tick_steps=64).serve([clone(target, 100, 0.0)], realtime=False)[0]
     mix = [clone(r, r.rid, 0.0) for r in reqs]
     eng = ServingEngine(storage=storage, tick_steps=37, max_slots=4)
