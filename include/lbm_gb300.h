@@ -86,10 +86,10 @@ typedef struct lbm_geometry {
   uint32_t edge_inlet_desc, edge_outlet_desc;
   int32_t n_bcnodes_edge;
   /* Reference velocity of the reference-shifted 16-bit storages
-   * (LBM_STORE_F16R, LBM_STORE_BF16R), inside (-0.5, 0.5): they keep
-   * f_i - c_i with c_i the equilibrium at rho = 1 and this velocity.  Ignored
-   * by the other storages; every call on one resident state must give the
-   * same value. */
+   * (LBM_STORE_F16R, LBM_STORE_BF16R): they keep f_i - c_i with c_i the
+   * equilibrium at rho = 1 and this velocity; every call on one resident state
+   * must give the same value.  The other storages do not use it (leave it 0);
+   * every call checks that it lies inside (-0.5, 0.5). */
   double dev_ref_ux, dev_ref_uy;
 } lbm_geometry;
 

@@ -272,7 +272,8 @@ class Lattice:
             else pop.cpu().numpy()
         return {"pending": np.asarray(0), "pop": pop,
                 "aux": self.aux[self.cur].cpu().numpy(), "t": np.asarray(self.t),
-                "storage": np.asarray(self.storage), "nx": np.asarray(self.nx), "ny": np.asarray(self.ny)}
+                "storage": np.asarray(self.storage), "nx": np.asarray(self.nx), "ny": np.asarray(self.ny),
+                "dev_ref": None if self.dev_ref is None else np.asarray(self.dev_ref, dtype=np.float64)}
 
     def restore(self, ck: dict):
         if int(ck["pending"]):
@@ -280,6 +281,11 @@ class Lattice:
             self.t = int(ck["t"])
             return self
         assert str(ck["storage"]) == self.storage and int(ck["nx"]) == self.nx and int(ck["ny"]) == self.ny
+        if self.dev_ref is not None:
+            # the stored numbers are deviations from the equilibrium at this reference velocity
+            saved = ck.get("dev_ref")
+            assert saved is not None and tuple(float(v) for v in np.asarray(saved)) == tuple(self.dev_ref), \
+                "the checkpoint was written with another reference velocity"
         self._init = None
         self.cur = 0
         pop = np.asarray(ck["pop"])
@@ -301,6 +307,7 @@ class Lattice:
             ck = {k: z[k] for k in z.files}
         ck.setdefault("rho", None)
         ck.setdefault("u", None)
+        ck.setdefault("dev_ref", None)
         if "pop" in ck and self.pop_dtype == torch.bfloat16:
             ck["pop"] = ck["pop"].view(np.uint16)
         return self.restore(ck)

@@ -52,18 +52,23 @@ def test_strouhal_and_decay_fit(pkg):
     assert abs(an.fit_decay_viscosity(amp, t[:2000], 0.01, 64) - 0.1666) < 1e-9
 
 
-@pytest.mark.parametrize("storage", ["fx64", "f64", "f16", "bf16"])
+@pytest.mark.parametrize("storage", ["fx64", "f64", "f16", "bf16", "f16r"])
 def test_checkpoint_resume_is_bit_exact(pkg, storage, tmp_path):
     S = pkg.scenarios
     f, rho, u, om, bnd = S.von_karman(120, 50, plate=10, re=80, seed=3)
-    a = pkg.Lattice(120, 50, om, bnd, storage=storage).set_state(f, rho, u).step(300)
+    kw = {"dev_ref": (0.1, 0.0)} if storage == "f16r" else {}
+    a = pkg.Lattice(120, 50, om, bnd, storage=storage, **kw).set_state(f, rho, u).step(300)
     path = os.path.join(tmp_path, "ck.npz")
     a.step(100)
     a.save(path)
     a.step(77)
-    b = pkg.Lattice(120, 50, om, bnd, storage=storage).load(path).step(77)
+    b = pkg.Lattice(120, 50, om, bnd, storage=storage, **kw).load(path).step(77)
     assert a.t == b.t == 477
     assert torch.equal(a.read()[0], b.read()[0])
+    if storage == "f16r":
+        # the stored numbers only mean something with the reference they were written with
+        with pytest.raises(AssertionError, match="reference velocity"):
+            pkg.Lattice(120, 50, om, bnd, storage=storage, dev_ref=(0.05, 0.0)).load(path)
 
 
 def test_frame_and_field_export(pkg, tmp_path):
