@@ -58,3 +58,9 @@ def test_phase_lag_is_not_pulled_by_a_growing_amplitude():
     ref = (1 + t / 2e4) * np.sin(2 * np.pi * t / 2600.0)
     assert bench.phase_lag(ref, ref.copy(), 2600, 10400) == 0
     assert bench.phase_lag(ref, (1 + (t + 25) / 2e4) * np.sin(2 * np.pi * (t + 25) / 2600.0), 2600, 10400) == 25
+
+
+def test_every_storage_has_a_bench_dtype():
+    import bench
+    from lattice_boltzmann_parallel_solver_gb300.lattice import BYTES_PER_NODE, STORAGES
+    assert set(bench.DTYPES) == set(STORAGES) == set(BYTES_PER_NODE)
